@@ -1,0 +1,392 @@
+#!/usr/bin/env python3
+"""Benchmark of the double-batched FFT hot path on GB300.
+
+Workload (the configuration the headline metric is quoted on): a double-batched 1d r2c
+followed by a c2r over an M x N x K float32 tensor, M = 8 (unit stride), K chosen so the
+real input is 1 GiB, for every N of the sweep {16,32,64,128,256,512,48,96,160,224,384,7,
+11,13}.  One step = the r2c and the c2r pass for every N of the sweep (28 launches).
+
+value  = algorithmic bytes of all passes / device time of the step (GB/s), where a pass
+         moves (N * 4 + (N/2+1) * 8) * M * K bytes (one read + one write, the reference's
+         benchmark/adapter.hpp:21-25,51-52 byte model); inputs are resident in HBM and are
+         1 GiB per pass, far larger than the 129 MB L2, so no flush is needed.
+e2e    = the same metric through the C ABI with pinned host buffers: each step copies the
+         inputs host->device, runs the passes and copies the results device->host.
+roofline = the engine kernels (every launch of the step): algorithmic bytes / summed
+         CUDA-event duration of the launches, against the measured HBM copy bandwidth.
+cpu_baseline = the oracle (C restatement of the reference's algorithm) on all host cores,
+         on a K-subset of the same workload.
+
+--impl reference times the reference's CPU implementation of the path (the oracle port;
+the reference's own kernels need an OpenCL/SYCL/Level Zero runtime that is not present)
+on the host cores with the same metric.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, 'double-batched-fft-library_gb300')
+for _p in (REPO, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+SWEEP_N = [16, 32, 64, 128, 256, 512, 48, 96, 160, 224, 384, 7, 11, 13]
+M_BATCH = 8
+REAL_BYTES = 1 << 30
+METRIC = 'GB/s vs HBM peak per N; plain vs split-TC form at rel-L2<=1e-6 vs FP64'
+
+
+def k_for(N, prec):
+    return REAL_BYTES // (prec * M_BATCH * N)
+
+
+def pass_bytes(N, K, prec, M=M_BATCH):
+    return (N * prec + (N // 2 + 1) * 2 * prec) * M * K
+
+
+def measured_peaks():
+    p = os.path.join(REPO, 'MEASURED_PEAKS.json')
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d['hbm_gbs']), 'measured'
+    return 6800.0, 'fallback'
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.gpu), '--query-gpu=' + self.FIELDS,
+                 '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(',')]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == 'active':
+                    reasons.add(nm)
+        return {'sm_mhz': float(np.median(sm)) if sm else None,
+                'sm_max_mhz': float(max(smax)) if smax else None,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return ws, rank, local
+
+
+# ------------------------------------------------------------------------------------------
+# CPU baseline (oracle port)
+
+
+def cpu_baseline(prec=4, budget_s=12.0, threads=None):
+    """Time the oracle's r2c+c2r over a K-subset of every N of the sweep on all host cores."""
+    from oracle import pyoracle as po
+
+    threads = threads or os.cpu_count() or 1
+    rng = np.random.default_rng(0)
+    rdt = np.float32 if prec == 4 else np.float64
+    cdt = np.complex64 if prec == 4 else np.complex128
+    total_bytes, total_t = 0, 0.0
+    per_n_budget = budget_s / len(SWEEP_N)
+    for N in SWEEP_N:
+        Kfull = k_for(N, prec)
+        K = max(2 * threads, min(Kfull, 4096 * 64 // N))
+        x = rng.standard_normal(M_BATCH * N * K).astype(rdt)
+        X = np.zeros(M_BATCH * (N // 2 + 1) * K, dtype=cdt)
+        y = np.zeros(M_BATCH * N * K, dtype=rdt)
+        reps, t_n = 0, 0.0
+        while t_n < per_n_budget or reps == 0:
+            t0 = time.perf_counter()
+            po.fft1d(po.R2C, po.FORWARD, M_BATCH, N, K, x, M_BATCH, M_BATCH * N, X, M_BATCH,
+                     M_BATCH * (N // 2 + 1), prec, threads)
+            po.fft1d(po.C2R, po.BACKWARD, M_BATCH, N, K, X, M_BATCH, M_BATCH * (N // 2 + 1), y,
+                     M_BATCH, M_BATCH * N, prec, threads)
+            t_n += time.perf_counter() - t0
+            reps += 1
+        total_bytes += 2 * pass_bytes(N, K, prec) * reps
+        total_t += t_n
+    return {'value': total_bytes / total_t / 1e9, 'unit': 'GB/s', 'cores': threads,
+            'kind': 'port',
+            'sample': 'oracle r2c+c2r, M=8, every N of the sweep, K-subset of %d..%d slices per N, '
+                      '%.0f s total' % (min(max(2 * threads, 4096 * 64 // n) for n in SWEEP_N),
+                                        max(max(2 * threads, 4096 * 64 // n) for n in SWEEP_N),
+                                        total_t)}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    prec = 4
+    res = None
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        cpu_baseline(prec, budget_s=2.0)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        res = cpu_baseline(prec, budget_s=max(3.0, 60.0 / max(1, args.steps)))
+        vals.append(res['value'])
+    elapsed = time.perf_counter() - t0
+    value = float(np.median(vals))
+    line = {
+        'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': 'GB/s', 'n_gpus': ws,
+        'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': elapsed / args.steps * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic: iid N(0,1) reals, seeded',
+        'config': {'workload': 'r2c+c2r round trip, M=8, 1 GiB real input per N, f32, '
+                               'N in ' + str(SWEEP_N) + ' (K-subset on the CPU)'},
+        'cpu_baseline': {'value': value, 'unit': 'GB/s', 'cores': res['cores'], 'kind': 'port',
+                         'sample': res['sample']},
+        'e2e': {'value': value, 'unit': 'GB/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+        'note': 'reference CPU path = C restatement of the reference kernels (oracle/); the '
+                'reference library itself needs an OpenCL/SYCL/Level Zero runtime',
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------------------------
+# GPU arm
+
+
+def run_ours(args):
+    import torch
+
+    import bbfft_gb300 as bb
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group('nccl')
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    prec = 4
+    hbm_peak, peak_kind = measured_peaks()
+
+    # one pair of buffers sized for the largest pass; K-slab per rank (weak scaling: every
+    # rank transforms a full 1 GiB tensor per N)
+    max_real = max(M_BATCH * N * k_for(N, prec) for N in SWEEP_N) * prec
+    max_cplx = max(M_BATCH * (N // 2 + 1) * k_for(N, prec) for N in SWEEP_N) * 2 * prec
+    xbuf = torch.empty(max_real // 4, dtype=torch.float32, device='cuda')
+    Xbuf = torch.empty(max_cplx // 4, dtype=torch.float32, device='cuda')
+    ybuf = torch.empty(max_real // 4, dtype=torch.float32, device='cuda')
+    g = torch.Generator(device='cuda')
+    g.manual_seed(1234 + rank)
+    xbuf.normal_(generator=g)
+
+    plans = []
+    total_bytes = 0
+    for N in SWEEP_N:
+        K = k_for(N, prec)
+        f = bb.configuration(1, [M_BATCH, N, K], precision=bb.F32, type=bb.R2C)
+        b = bb.configuration(1, [M_BATCH, N, K], precision=bb.F32, type=bb.C2R,
+                             direction=bb.BACKWARD)
+        plans.append((N, K, bb.Plan(f, stream=sptr), bb.Plan(b, stream=sptr)))
+        total_bytes += 2 * pass_bytes(N, K, prec)
+
+    xp, Xp, yp = xbuf.data_ptr(), Xbuf.data_ptr(), ybuf.data_ptr()
+
+    def step(events=None):
+        for i, (N, K, pf, pb) in enumerate(plans):
+            if events is not None:
+                events[4 * i].record(stream)
+            pf.execute(xp, Xp)
+            if events is not None:
+                events[4 * i + 1].record(stream)
+                events[4 * i + 2].record(stream)
+            pb.execute(Xp, yp)
+            if events is not None:
+                events[4 * i + 3].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4 * len(plans))]
+          for _ in range(args.steps)]
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for s in range(args.steps):
+        step(ev[s])
+    stop.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    t_ms = start.elapsed_time(stop)
+    if dist:
+        tt = torch.tensor([t_ms], device='cuda')
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_ms = float(tt.item())
+        dist.barrier()
+    ms_per_step = t_ms / args.steps
+    value = total_bytes * ws / (ms_per_step * 1e-3) / 1e9
+
+    # per-launch durations (events around each launch inside the timed region)
+    per_n = []
+    kernel_ms = 0.0
+    for i, (N, K, _, _) in enumerate(plans):
+        tf = np.mean([ev[s][4 * i].elapsed_time(ev[s][4 * i + 1]) for s in range(args.steps)])
+        tb = np.mean([ev[s][4 * i + 2].elapsed_time(ev[s][4 * i + 3]) for s in range(args.steps)])
+        kernel_ms += tf + tb
+        pbytes = pass_bytes(N, K, prec)
+        per_n.append({'N': N, 'K': K, 'r2c_gbs': round(pbytes / tf / 1e6, 1),
+                      'c2r_gbs': round(pbytes / tb / 1e6, 1),
+                      'r2c_frac': round(pbytes / tf / 1e6 / hbm_peak, 3),
+                      'c2r_frac': round(pbytes / tb / 1e6 / hbm_peak, 3)})
+    achieved = total_bytes / (kernel_ms * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(REPO, 'profiles', 'traffic.json')
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get('bytes_per_step')
+
+    # end-to-end through the C ABI with pinned host buffers (rank-local)
+    e2e = run_e2e(bb, torch, plans, prec, sptr, stream, args)
+
+    line = {
+        'metric': METRIC, 'value': round(value, 1), 'unit': 'GB/s', 'n_gpus': ws,
+        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms_per_step, 4),
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+        'data': 'synthetic: iid N(0,1) float32 reals from a seeded generator',
+        'config': {'workload': 'r2c+c2r round trip, M=8, 1 GiB real input per N, f32',
+                   'N': SWEEP_N, 'M': M_BATCH, 'l2': 'inputs of 1 GiB per pass > L2, no flush',
+                   'parallelism': 'K-slab per rank, no collectives' if ws > 1 else 'single GPU'},
+        'roofline': {'bound': 'hbm', 'achieved': round(achieved, 1), 'peak': hbm_peak,
+                     'unit': 'GB/s', 'frac': round(achieved / hbm_peak, 4), 'traffic': traffic,
+                     'peak_kind': peak_kind, 'kernel': 'gbfft::fft_kernel<float, kind> (all '
+                     'launches of the step; algorithmic bytes = one read + one write)'},
+        'per_n': per_n,
+        'clocks': clk,
+        'e2e': e2e,
+        'gpu_launches': 2 * len(plans) * args.steps,
+    }
+    if rank == 0 and not args.no_cpu:
+        line['cpu_baseline'] = cpu_baseline(prec, budget_s=args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_e2e(bb, torch, plans, prec, sptr, stream, args):
+    """Same workload through the C ABI with pinned host buffers: H2D, r2c, c2r, D2H per pass."""
+    # a reduced sweep keeps the host buffers small: every N, K-slab of 1/8 of the tensor
+    frac = 8
+    total_bytes, h2d, d2h = 0, 0, 0
+    items = []
+    for (N, K, _, _) in plans:
+        Ks = max(1, K // frac)
+        f = bb.configuration(1, [M_BATCH, N, Ks], precision=bb.F32, type=bb.R2C)
+        b = bb.configuration(1, [M_BATCH, N, Ks], precision=bb.F32, type=bb.C2R,
+                             direction=bb.BACKWARD)
+        nreal = M_BATCH * N * Ks
+        ncplx = M_BATCH * (N // 2 + 1) * Ks
+        items.append((bb.Plan(f, stream=sptr), bb.Plan(b, stream=sptr), nreal, ncplx))
+        total_bytes += 2 * pass_bytes(N, Ks, prec)
+        h2d += nreal * prec
+        d2h += nreal * prec
+    maxr = max(i[2] for i in items)
+    maxc = max(i[3] for i in items)
+    host_in = torch.empty(maxr, dtype=torch.float32, pin_memory=True)
+    host_in.normal_()
+    host_out = torch.empty(maxr, dtype=torch.float32, pin_memory=True)
+    d_in = torch.empty(maxr, dtype=torch.float32, device='cuda')
+    d_X = torch.empty(2 * maxc, dtype=torch.float32, device='cuda')
+    d_out = torch.empty(maxr, dtype=torch.float32, device='cuda')
+
+    def step():
+        for pf, pb, nreal, ncplx in items:
+            d_in[:nreal].copy_(host_in[:nreal], non_blocking=True)
+            pf.execute(d_in.data_ptr(), d_X.data_ptr())
+            pb.execute(d_X.data_ptr(), d_out.data_ptr())
+            host_out[:nreal].copy_(d_out[:nreal], non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    s0 = torch.cuda.Event(enable_timing=True)
+    s1 = torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    for _ in range(args.steps):
+        step()
+    s1.record(stream)
+    torch.cuda.synchronize()
+    ms = s0.elapsed_time(s1) / args.steps
+    return {'value': round(total_bytes / (ms * 1e-3) / 1e9, 1), 'unit': 'GB/s',
+            'h2d_bytes_per_step': h2d, 'd2h_bytes_per_step': d2h,
+            'workload': 'same sweep at 1/8 of K per N (128 MiB real input per N), pinned host '
+                        'buffers, copies inside the timed region'}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--cpu-seconds', type=float, default=15.0)
+    args = ap.parse_args()
+    if args.impl == 'reference':
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == '__main__':
+    main()

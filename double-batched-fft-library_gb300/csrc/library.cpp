@@ -1,0 +1,1130 @@
+// Host side of the GB300 double-batched FFT library: plan creation (algorithm
+// selection and blocking), nd chaining, execution, plan caches and the NVRTC path for
+// user callbacks.  Everything is exported through the C ABI of bbfft_gb300.h.
+//
+// Correspondence with the reference (intel/double-batched-fft-library 0.5.1):
+//   select_fft_algorithm           src/common/algorithm.hpp:20-30      -> make_plan_impl
+//   select_1d_fft_algorithm        src/common/algorithm_1d.hpp:19-36   -> make_1d_pass
+//   small_batch_fft / factor2_slm  src/common/algorithm/*.hpp          -> one engine, blocking below
+//   nd_fft                         src/common/algorithm/nd_fft.hpp     -> make_nd
+//   jit_cache / jit_cache_all      src/base/jit_cache*.cpp             -> bbfft_cache_s
+//   aot_cache                      src/base/aot_cache.cpp              -> bbfft_cache_s (aot)
+#include "config.hpp"
+#include "kernels.hpp"
+#include "params.h"
+
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <set>
+#include <sstream>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "engine_src.inc" // kEngineSource: the device engine as text, for NVRTC
+
+namespace gbfft {
+
+// ------------------------------------------------------------------------------------------
+// errors
+
+thread_local std::string tl_error;
+
+#define GB_CUDA(call)                                                                            \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess) {                                                                 \
+            throw status_error(BBFFT_CUDA_ERROR,                                                 \
+                               std::string(#call) + " failed: " + cudaGetErrorString(e_));       \
+        }                                                                                        \
+    } while (0)
+
+[[noreturn]] void bad_config(std::string const &what) {
+    throw status_error(BBFFT_BAD_CONFIGURATION, what);
+}
+
+template <class F> int guarded(F &&f) {
+    try {
+        f();
+        return BBFFT_SUCCESS;
+    } catch (status_error const &e) {
+        tl_error = e.what();
+        return e.status();
+    } catch (std::bad_alloc const &) {
+        tl_error = "out of host memory";
+        return BBFFT_OUT_OF_MEMORY;
+    } catch (std::exception const &e) {
+        tl_error = e.what();
+        return BBFFT_INTERNAL_ERROR;
+    } catch (...) {
+        tl_error = "unknown error";
+        return BBFFT_INTERNAL_ERROR;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// device memory
+
+struct device_buffer {
+    void *ptr = nullptr;
+    std::size_t bytes = 0;
+    device_buffer(std::size_t n) : bytes(n) {
+        if (n) {
+            cudaError_t e = cudaMalloc(&ptr, n);
+            if (e != cudaSuccess) {
+                (void)cudaGetLastError();
+                throw status_error(BBFFT_OUT_OF_MEMORY,
+                                   "cudaMalloc(" + std::to_string(n) + ") failed: " +
+                                       cudaGetErrorString(e));
+            }
+        }
+    }
+    ~device_buffer() {
+        if (ptr) {
+            cudaFree(ptr);
+        }
+    }
+    device_buffer(device_buffer const &) = delete;
+    device_buffer &operator=(device_buffer const &) = delete;
+};
+
+// Twiddle tables w_Nt^{-i} = exp(-2 pi i i / Nt), i = 0..Nt-1, evaluated in long double
+// and rounded once to the plan precision.  Shared between plans of one device.
+static void twiddle_value(int i, int Nt, long double &c, long double &s) {
+    // exact values at multiples of pi/2
+    int q = i % Nt;
+    if ((4LL * q) % Nt == 0) {
+        int quad = static_cast<int>((4LL * q) / Nt);
+        static const int cs[4][2] = {{1, 0}, {0, 1}, {-1, 0}, {0, -1}};
+        c = cs[quad][0];
+        s = cs[quad][1];
+        return;
+    }
+    long double const tau = 6.283185307179586476925286766559005768L;
+    long double a = tau * static_cast<long double>(q) / static_cast<long double>(Nt);
+    c = std::cos(a);
+    s = std::sin(a);
+}
+
+std::shared_ptr<device_buffer> get_twiddles(int device, int prec, int Nt) {
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, int>, std::weak_ptr<device_buffer>> tables;
+    std::lock_guard<std::mutex> lock(mu);
+    auto key = std::make_tuple(device, prec, Nt);
+    auto it = tables.find(key);
+    if (it != tables.end()) {
+        if (auto sp = it->second.lock()) {
+            return sp;
+        }
+    }
+    auto buf = std::make_shared<device_buffer>(static_cast<std::size_t>(Nt) * 2 * prec);
+    if (prec == 4) {
+        std::vector<float> h(2 * Nt);
+        for (int i = 0; i < Nt; ++i) {
+            long double c, s;
+            twiddle_value(i, Nt, c, s);
+            h[2 * i] = static_cast<float>(c);
+            h[2 * i + 1] = static_cast<float>(-s);
+        }
+        GB_CUDA(cudaMemcpy(buf->ptr, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<double> h(2 * Nt);
+        for (int i = 0; i < Nt; ++i) {
+            long double c, s;
+            twiddle_value(i, Nt, c, s);
+            h[2 * i] = static_cast<double>(c);
+            h[2 * i + 1] = static_cast<double>(-s);
+        }
+        GB_CUDA(cudaMemcpy(buf->ptr, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    tables[key] = buf;
+    return buf;
+}
+
+// ------------------------------------------------------------------------------------------
+// modules (NVRTC output or registered AOT images)
+
+struct module {
+    cudaLibrary_t lib = nullptr;
+    ~module() {
+        if (lib) {
+            cudaLibraryUnload(lib);
+        }
+    }
+    cudaKernel_t kernel(std::string const &name) const {
+        cudaKernel_t k = nullptr;
+        cudaError_t e = cudaLibraryGetKernel(&k, lib, name.c_str());
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            return nullptr;
+        }
+        return k;
+    }
+};
+
+} // namespace gbfft
+
+struct bbfft_cache_s {
+    bool aot = false;
+    std::mutex mu;
+    std::unordered_map<std::string, std::shared_ptr<gbfft::module>> jit; // key: name@device
+    struct aot_module {
+        std::shared_ptr<gbfft::module> mod;
+        std::set<std::string> names;
+        int device;
+    };
+    std::vector<aot_module> aot_modules;
+    std::atomic<uint64_t> hits{0}, misses{0};
+
+    std::shared_ptr<gbfft::module> get(std::string const &name, int device) {
+        std::lock_guard<std::mutex> lock(mu);
+        std::shared_ptr<gbfft::module> r;
+        if (aot) {
+            for (auto const &m : aot_modules) {
+                if (m.device == device && m.names.count(name)) {
+                    r = m.mod;
+                    break;
+                }
+            }
+        } else {
+            auto it = jit.find(name + "@" + std::to_string(device));
+            if (it != jit.end()) {
+                r = it->second;
+            }
+        }
+        (r ? hits : misses)++;
+        return r;
+    }
+    void store(std::string const &name, int device, std::shared_ptr<gbfft::module> m) {
+        if (aot) {
+            return; // reference aot_cache::store is a no-op (src/base/aot_cache.cpp:24)
+        }
+        std::lock_guard<std::mutex> lock(mu);
+        jit[name + "@" + std::to_string(device)] = std::move(m);
+    }
+};
+
+namespace gbfft {
+
+static std::string nvrtc_arch(int device) {
+    cudaDeviceProp prop;
+    GB_CUDA(cudaGetDeviceProperties(&prop, device));
+    std::string arch = "sm_" + std::to_string(prop.major) + std::to_string(prop.minor);
+    if (prop.major >= 9) {
+        arch += "a";
+    }
+    return "--gpu-architecture=" + arch;
+}
+
+std::shared_ptr<module> nvrtc_build(std::string const &source, std::string const &name,
+                                    int device) {
+    nvrtcProgram prog;
+    if (nvrtcCreateProgram(&prog, source.c_str(), (name + ".cu").c_str(), 0, nullptr, nullptr) !=
+        NVRTC_SUCCESS) {
+        throw status_error(BBFFT_COMPILE_ERROR, "nvrtcCreateProgram failed");
+    }
+    std::string arch = nvrtc_arch(device);
+    const char *opts[] = {arch.c_str(), "-std=c++17", "-lineinfo", "-DGBFFT_JIT=1"};
+    nvrtcResult rc = nvrtcCompileProgram(prog, 4, opts);
+    std::size_t log_size = 0;
+    nvrtcGetProgramLogSize(prog, &log_size);
+    std::string log(log_size, '\0');
+    if (log_size) {
+        nvrtcGetProgramLog(prog, &log[0]);
+    }
+    if (rc != NVRTC_SUCCESS) {
+        nvrtcDestroyProgram(&prog);
+        throw status_error(BBFFT_COMPILE_ERROR, "NVRTC compilation of " + name + " failed:\n" + log);
+    }
+    std::size_t cubin_size = 0;
+    nvrtcGetCUBINSize(prog, &cubin_size);
+    std::vector<char> cubin(cubin_size);
+    nvrtcGetCUBIN(prog, cubin.data());
+    nvrtcDestroyProgram(&prog);
+    auto m = std::make_shared<module>();
+    GB_CUDA(cudaLibraryLoadData(&m->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
+    return m;
+}
+
+// ------------------------------------------------------------------------------------------
+// algorithm selection and blocking
+
+static bool unrolled(int P) { return P == 1 || (P >= 2 && P <= 13) || P == 16; }
+
+static std::vector<int> prime_factors(int n) {
+    std::vector<int> f;
+    for (int p = 2; n > 1;) {
+        if (n % p == 0) {
+            f.push_back(p);
+            n /= p;
+        } else {
+            ++p;
+        }
+    }
+    return f;
+}
+
+// Radices for an Nc-point complex FFT: few stages, unrolled butterflies where possible.
+std::vector<int> choose_radices(int Nc) {
+    if (Nc == 1) {
+        return {1};
+    }
+    auto f = prime_factors(Nc);
+    int c2 = 0, c3 = 0;
+    std::vector<int> odd, big;
+    for (int p : f) {
+        if (p == 2) {
+            ++c2;
+        } else if (p == 3) {
+            ++c3;
+        } else if (p <= 13) {
+            odd.push_back(p);
+        } else {
+            big.push_back(p);
+        }
+    }
+    std::vector<int> r;
+    while (c3 >= 2) {
+        r.push_back(9);
+        c3 -= 2;
+    }
+    if (c3 == 1) {
+        if (c2 >= 2 && c2 != 3 && c2 != 6) { // keep 8 / 8x8 for the power-of-two part
+            r.push_back(12);
+            c2 -= 2;
+        } else if (c2 >= 1) {
+            r.push_back(6);
+            c2 -= 1;
+        } else {
+            r.push_back(3);
+        }
+    }
+    for (int p : odd) {
+        if (p == 5 && c2 >= 1 && c2 % 3 == 1) {
+            r.push_back(10);
+            c2 -= 1;
+        } else {
+            r.push_back(p);
+        }
+    }
+    if (c2 > 0) {
+        int chunks = (c2 + 3) / 4;
+        for (int i = 0; i < chunks; ++i) {
+            int bits = c2 / chunks + (i < c2 % chunks ? 1 : 0);
+            r.push_back(1 << bits);
+        }
+    }
+    std::sort(r.begin(), r.end(), [](int a, int b) { return a > b; });
+    for (int p : big) {
+        r.push_back(p); // generic radices last: they need a shared-memory source
+    }
+    return r;
+}
+
+struct pass {
+    int prec = 4;
+    int kind = kind_c2c;
+    fft_params p = {};
+    unsigned grid = 0;
+    unsigned block = 0;
+    std::size_t smem = 0;
+    const void *func = nullptr;
+    std::shared_ptr<module> mod;
+    std::shared_ptr<device_buffer> tw;
+    bool inplace_ok = true;
+    std::string identifier;
+    int in_sel = 0;  // 0: user input, 2: temporary
+    int out_sel = 1; // 1: user output, 2: temporary
+};
+
+struct pass_request {
+    int prec, type, dir;
+    bool adjoint = false;
+    long long M, N, K;
+    long long is1, is2, os1, os2;
+    const char *cb_source = nullptr;
+    std::size_t cb_length = 0;
+    const char *load_fn = nullptr;
+    const char *store_fn = nullptr;
+    // tuning overrides
+    std::vector<int> radices;
+    int T = 0, Mb = 0, Kb = 0;
+};
+
+static int max_optin_smem(int device) {
+    int v = 0;
+    GB_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+    return v;
+}
+
+static std::string c_ident(std::string s) {
+    for (auto &ch : s) {
+        if (!std::isalnum(static_cast<unsigned char>(ch)) && ch != '_') {
+            ch = '_';
+        }
+    }
+    return s;
+}
+
+static uint64_t fnv1a(const char *data, std::size_t n) {
+    uint64_t h = 1469598103934665603ull;
+    for (std::size_t i = 0; i < n; ++i) {
+        h ^= static_cast<unsigned char>(data[i]);
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+
+static char const *kind_name(int kind) {
+    switch (kind) {
+    case kind_c2c:
+        return "c2c";
+    case kind_r2c_half:
+        return "r2ch";
+    case kind_r2c_full:
+        return "r2cf";
+    case kind_c2r_half:
+        return "c2rh";
+    case kind_c2r_full:
+        return "c2rf";
+    }
+    return "?";
+}
+
+pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
+    pass ps;
+    ps.prec = q.prec;
+    bool is_real = q.type != BBFFT_C2C;
+    int N = static_cast<int>(q.N);
+    bool even = N % 2 == 0;
+    // kernel kind; the adjoint of r2c runs the c2r engine and vice versa
+    int eff_type = q.type;
+    int flags = 0;
+    if (q.adjoint) {
+        if (q.type == BBFFT_R2C) {
+            eff_type = BBFFT_C2R;
+            flags |= flag_adj_r2c;
+        } else if (q.type == BBFFT_C2R) {
+            eff_type = BBFFT_R2C;
+            flags |= flag_adj_c2r;
+        }
+    }
+    int dir = q.adjoint && q.type == BBFFT_C2C ? -q.dir : q.dir;
+    switch (eff_type) {
+    case BBFFT_C2C:
+        ps.kind = kind_c2c;
+        if (dir == BBFFT_BACKWARD) {
+            flags |= flag_conj_in | flag_conj_out;
+        }
+        break;
+    case BBFFT_R2C:
+        ps.kind = even ? kind_r2c_half : kind_r2c_full;
+        break;
+    case BBFFT_C2R:
+        ps.kind = even ? kind_c2r_half : kind_c2r_full;
+        break;
+    }
+    int Nc = (is_real && even) ? N / 2 : N;
+    int Nt = (is_real && even) ? N : Nc;
+
+    std::vector<int> rad = q.radices.empty() ? choose_radices(Nc) : q.radices;
+    {
+        long long prod = 1;
+        for (int r : rad) {
+            if (r < 1) {
+                bad_config("radix must be positive");
+            }
+            prod *= r;
+        }
+        if (prod != Nc) {
+            bad_config("product of radices must equal the complex FFT length " + std::to_string(Nc));
+        }
+    }
+    bool pre = ps.kind == kind_c2r_half;
+    bool post = ps.kind == kind_r2c_half;
+    // a generic (non-unrolled) first stage needs a shared-memory source
+    if (!pre && !unrolled(rad.front())) {
+        rad.insert(rad.begin(), 1);
+    }
+    // real transforms must finish all global reads of a tile before the first global write
+    // (in-place safety): with a single global->global stage, add a shared round trip
+    if (is_real && !pre && !post && rad.size() == 1) {
+        rad.push_back(1);
+    }
+    if (rad.size() > static_cast<std::size_t>(max_stages)) {
+        bad_config("too many stages");
+    }
+    int L = static_cast<int>(rad.size());
+    int nbuf = 1;
+    for (int s = 0; s < L; ++s) {
+        bool src_g = s == 0 && !pre;
+        bool dst_g = s == L - 1 && !post;
+        if (!src_g && !dst_g) {
+            nbuf = 2;
+        }
+    }
+    int pu = 1;
+    for (int r : rad) {
+        if (unrolled(r)) {
+            pu = std::max(pu, r);
+        }
+    }
+    int T = q.T > 0 ? q.T : std::max(1, Nc / pu);
+    if (pu == 1) {
+        T = std::min(Nc, 64);
+    }
+    T = std::min(T, 512);
+
+    long long M = q.M, K = q.K;
+    int Mb;
+    if (q.Mb > 0) {
+        Mb = static_cast<int>(std::min<long long>(q.Mb, M));
+    } else if (M == 1) {
+        Mb = 1;
+    } else if (is_real && M <= 64 && M * T <= 512) {
+        Mb = static_cast<int>(M);
+    } else {
+        Mb = static_cast<int>(std::min<long long>(M, 32));
+    }
+    while (Mb > 1 && Mb * T > 512) {
+        Mb = (Mb + 1) / 2;
+    }
+    std::size_t celem = 2 * static_cast<std::size_t>(q.prec);
+    auto buf_elems = [&](int kb) {
+        long long n = static_cast<long long>(kb) * Nc * Mb;
+        long long last = n - 1;
+        long long padded = q.prec == 4 ? last + (last >> 4) : last + (last >> 3);
+        return padded + 1;
+    };
+    int Kb = q.Kb > 0 ? q.Kb : std::max(1, 256 / (Mb * T));
+    Kb = static_cast<int>(std::min<long long>(Kb, K));
+    Kb = std::max(Kb, 1);
+    while (Kb * Mb * T > 512 && Kb > 1) {
+        Kb /= 2;
+    }
+    std::size_t const soft_limit = 96 * 1024;
+    while (Kb > 1 && nbuf * buf_elems(Kb) * celem > soft_limit) {
+        Kb /= 2;
+    }
+    std::size_t smem = nbuf * buf_elems(Kb) * celem;
+    if (smem > static_cast<std::size_t>(max_optin_smem(device))) {
+        bad_config("FFT length " + std::to_string(N) + " needs " + std::to_string(smem) +
+                   " bytes of shared memory per block, more than the device provides");
+    }
+
+    fft_params &p = ps.p;
+    p.M = M;
+    p.K = K;
+    p.is1 = q.is1;
+    p.is2 = q.is2;
+    p.os1 = q.os1;
+    p.os2 = q.os2;
+    p.N = N;
+    p.Nc = Nc;
+    p.Nt = Nt;
+    p.L = L;
+    for (int s = 0; s < L; ++s) {
+        p.radix[s] = rad[s];
+    }
+    p.T = T;
+    p.Mb = Mb;
+    p.Kb = Kb;
+    p.m_tiles = static_cast<int>((M + Mb - 1) / Mb);
+    p.flags = flags;
+    p.nbuf = nbuf;
+    p.buf_elems = static_cast<int>(buf_elems(Kb));
+    p.scale = 1.0;
+    long long k_tiles = (K + Kb - 1) / Kb;
+    if (static_cast<long long>(p.m_tiles) * k_tiles > 0x7fffffffLL) {
+        bad_config("tensor too large for one launch");
+    }
+    ps.grid = static_cast<unsigned>(p.m_tiles * k_tiles);
+    ps.block = static_cast<unsigned>(Mb * T * Kb);
+    ps.smem = smem;
+    ps.inplace_ok = !is_real || Mb >= M;
+    ps.tw = get_twiddles(device, q.prec, Nt);
+    p.tw = ps.tw->ptr;
+
+    std::ostringstream id;
+    id << "gbfft_f" << q.prec * 8 << "_" << kind_name(ps.kind) << "_fl" << flags << "_M" << M
+       << "_Mb" << Mb << "_N" << N << "_r";
+    for (int s = 0; s < L; ++s) {
+        id << (s ? "x" : "") << rad[s];
+    }
+    id << "_T" << T << "_Kb" << Kb << "_is" << q.is1 << "_" << q.is2 << "_os" << q.os1 << "_"
+       << q.os2;
+    bool has_cb = (q.load_fn && *q.load_fn) || (q.store_fn && *q.store_fn);
+    if (q.load_fn && *q.load_fn) {
+        id << "_" << q.load_fn;
+    }
+    if (q.store_fn && *q.store_fn) {
+        id << "_" << q.store_fn;
+    }
+    ps.identifier = c_ident(id.str());
+
+    if (!has_cb) {
+        ps.func = q.prec == 4 ? kernel_f32(ps.kind) : kernel_f64(ps.kind);
+        if (!ps.func) {
+            throw status_error(BBFFT_INTERNAL_ERROR, "kernel not found");
+        }
+    } else {
+        if (!q.cb_source || q.cb_length == 0) {
+            bad_config("callback function named but no callback source given");
+        }
+        // The compiled code depends on precision, kind and the callbacks only, so modules
+        // are shared between plans of different shapes.
+        std::ostringstream key;
+        key << "gbfft_cb_f" << q.prec * 8 << "_" << kind_name(ps.kind) << "_"
+            << (q.load_fn ? q.load_fn : "") << "_" << (q.store_fn ? q.store_fn : "") << "_"
+            << std::hex << fnv1a(q.cb_source, q.cb_length);
+        std::string kname = c_ident(key.str());
+        std::shared_ptr<module> mod;
+        if (cache) {
+            mod = cache->get(kname, device);
+        }
+        if (!mod) {
+            std::ostringstream src;
+            src << "typedef decltype(sizeof(0)) size_t;\n";
+            src << kEngineSource << "\n";
+            src << std::string(q.cb_source, q.cb_length) << "\n";
+            src << "struct gbfft_user_io {\n"
+                << "  template <class T> static __device__ __forceinline__ T load(const T *p, "
+                   "unsigned long long off) {\n";
+            if (q.load_fn && *q.load_fn) {
+                src << "    return " << q.load_fn << "(const_cast<T *>(p), (size_t)off);\n";
+            } else {
+                src << "    return p[off];\n";
+            }
+            src << "  }\n  template <class T> static __device__ __forceinline__ void store(T *p, "
+                   "unsigned long long off, T v) {\n";
+            if (q.store_fn && *q.store_fn) {
+                src << "    " << q.store_fn << "(p, (size_t)off, v);\n";
+            } else {
+                src << "    p[off] = v;\n";
+            }
+            src << "  }\n};\n";
+            src << "extern \"C\" __global__ void __launch_bounds__(512) " << kname
+                << "(const __grid_constant__ gbfft::fft_params p) {\n"
+                << "  gbfft::fft_tile<" << (q.prec == 4 ? "float" : "double") << ", "
+                << ps.kind << ", gbfft_user_io>(p);\n}\n";
+            mod = nvrtc_build(src.str(), kname, device);
+            if (cache) {
+                cache->store(kname, device, mod);
+            }
+        }
+        cudaKernel_t k = mod->kernel(kname);
+        if (!k) {
+            throw status_error(BBFFT_INTERNAL_ERROR, "kernel " + kname + " not in module");
+        }
+        ps.mod = mod;
+        ps.func = reinterpret_cast<const void *>(k);
+    }
+    if (smem > 48 * 1024) {
+        GB_CUDA(cudaFuncSetAttribute(ps.func, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem)));
+    }
+    return ps;
+}
+
+} // namespace gbfft
+
+// ------------------------------------------------------------------------------------------
+// plans
+
+struct bbfft_plan_s {
+    std::atomic<int> refs{1};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<gbfft::pass> passes;
+    std::shared_ptr<gbfft::device_buffer> tmp;
+    bool inplace_ok = true;
+    bool jit = false;
+};
+
+namespace gbfft {
+
+static void validate(bbfft_configuration const &cfg) {
+    if (cfg.dim < 1 || cfg.dim > max_fft_dim) {
+        bad_config("Unsupported FFT dimension: " + std::to_string(cfg.dim));
+    }
+    if (cfg.precision != BBFFT_PRECISION_F32 && cfg.precision != BBFFT_PRECISION_F64) {
+        bad_config("Unsupported precision");
+    }
+    if (cfg.type != BBFFT_C2C && cfg.type != BBFFT_R2C && cfg.type != BBFFT_C2R) {
+        bad_config("Unsupported transform type");
+    }
+    if (cfg.direction != BBFFT_FORWARD && cfg.direction != BBFFT_BACKWARD) {
+        bad_config("Unsupported direction");
+    }
+    if ((cfg.type == BBFFT_R2C && cfg.direction != BBFFT_FORWARD) ||
+        (cfg.type == BBFFT_C2R && cfg.direction != BBFFT_BACKWARD)) {
+        bad_config("r2c direction must be forward and c2r direction must be backward");
+    }
+    for (unsigned d = 0; d < cfg.dim + 2; ++d) {
+        if (cfg.shape[d] == 0) {
+            bad_config("tensor shape entries must be positive");
+        }
+    }
+    if (cfg.istride[0] != 1 || cfg.ostride[0] != 1) {
+        bad_config("stride s0 != 1 is not supported");
+    }
+    if (cfg.compute != BBFFT_COMPUTE_NATIVE) {
+        bad_config("compute mode not available for this configuration");
+    }
+}
+
+static void make_plan_impl(bbfft_configuration const &cfg, cudaStream_t stream,
+                           bbfft_cache_s *cache, bool adjoint, bbfft_plan_s &plan,
+                           pass_request const *tuning) {
+    validate(cfg);
+    bool has_cb = (cfg.load_function && *cfg.load_function) ||
+                  (cfg.store_function && *cfg.store_function);
+    stride_t shape = to_array(cfg.shape);
+    auto is_default = [&](bool inplace) {
+        stride_t di = default_istride(cfg.dim, shape, cfg.type, inplace);
+        stride_t dout = default_ostride(cfg.dim, shape, cfg.type, inplace);
+        for (unsigned d = 0; d < cfg.dim + 2; ++d) {
+            if (cfg.istride[d] != di[d] || cfg.ostride[d] != dout[d]) {
+                return false;
+            }
+        }
+        return true;
+    };
+    if (cfg.dim > 1) {
+        if (has_cb) {
+            bad_config("User modules are unsuported for FFT dimension > 1.");
+        }
+        if (!is_default(false) && !is_default(true)) {
+            bad_config("Only default tensor layouts are supported for the nd_fft.");
+        }
+    }
+    if (adjoint && has_cb) {
+        bad_config("callbacks are not supported for adjoint plans");
+    }
+    GB_CUDA(cudaGetDevice(&plan.device));
+    plan.stream = stream;
+    if (cfg.dim == 1) {
+        pass_request q = tuning ? *tuning : pass_request{};
+        q.prec = cfg.precision;
+        q.type = cfg.type;
+        q.dir = cfg.direction;
+        q.adjoint = adjoint;
+        q.M = static_cast<long long>(cfg.shape[0]);
+        q.N = static_cast<long long>(cfg.shape[1]);
+        q.K = static_cast<long long>(cfg.shape[2]);
+        if (!adjoint) {
+            q.is1 = cfg.istride[1];
+            q.is2 = cfg.istride[2];
+            q.os1 = cfg.ostride[1];
+            q.os2 = cfg.ostride[2];
+        } else { // the adjoint maps the output layout back to the input layout
+            q.is1 = cfg.ostride[1];
+            q.is2 = cfg.ostride[2];
+            q.os1 = cfg.istride[1];
+            q.os2 = cfg.istride[2];
+        }
+        q.cb_source = cfg.callback_source;
+        q.cb_length = cfg.callback_length;
+        q.load_fn = cfg.load_function;
+        q.store_fn = cfg.store_function;
+        plan.passes.push_back(make_1d_pass(q, plan.device, cache));
+        plan.inplace_ok = plan.passes.back().inplace_ok;
+        plan.jit = has_cb;
+        return;
+    }
+    // ---- nd: chain of 1d passes (reference src/common/algorithm/nd_fft.hpp:27-130) ----
+    bool inplace_layout = is_default(true);
+    bool is_real = cfg.type != BBFFT_C2C;
+    unsigned dim = cfg.dim;
+    auto nd_complex = [&](unsigned d) -> long long {
+        return d == 0 && is_real ? cfg.shape[1] / 2 + 1 : cfg.shape[d + 1];
+    };
+    auto nd_real = [&](unsigned d) -> long long {
+        return d == 0 && is_real && inplace_layout ? 2 * (cfg.shape[1] / 2 + 1) : cfg.shape[d + 1];
+    };
+    long long Ntot = 1;
+    for (unsigned d = 0; d < dim; ++d) {
+        Ntot *= nd_complex(d);
+    }
+    std::vector<pass_request> reqs(dim);
+    long long M = cfg.shape[0];
+    long long K = Ntot * static_cast<long long>(cfg.shape[dim + 1]);
+    for (unsigned d = 0; d < dim; ++d) {
+        long long Nd = cfg.shape[d + 1];
+        long long Ndc = nd_complex(d);
+        K /= Ndc;
+        pass_request &q = reqs[d];
+        q.prec = cfg.precision;
+        q.type = d == 0 ? cfg.type : BBFFT_C2C;
+        q.dir = cfg.direction;
+        q.adjoint = adjoint;
+        q.M = M;
+        q.N = Nd;
+        q.K = K;
+        q.is1 = M;
+        q.is2 = M * nd_real(d);
+        q.os1 = M;
+        q.os2 = M * Ndc;
+        M *= Ndc;
+    }
+    // forward execution order: c2r starts with the outer dimensions and swaps the layouts
+    // of every pass (nd_fft.hpp:100-108)
+    std::vector<pass_request> order;
+    bool reverse = cfg.type == BBFFT_C2R;
+    for (unsigned d = 0; d < dim; ++d) {
+        pass_request q = reverse ? reqs[dim - 1 - d] : reqs[d];
+        q.adjoint = false;
+        if (reverse) {
+            std::swap(q.is1, q.os1);
+            std::swap(q.is2, q.os2);
+        }
+        order.push_back(q);
+    }
+    // the adjoint runs the adjoints of the passes in reverse order, each mapping the
+    // layout of its forward output back to the layout of its forward input
+    if (adjoint) {
+        std::reverse(order.begin(), order.end());
+        for (auto &q : order) {
+            q.adjoint = true;
+            std::swap(q.is1, q.os1);
+            std::swap(q.is2, q.os2);
+        }
+    }
+    for (auto &q : order) {
+        plan.passes.push_back(make_1d_pass(q, plan.device, cache));
+    }
+    // temporary buffer if the input is larger than the output (nd_fft.hpp:114-125)
+    std::size_t real_b = cfg.precision, cplx_b = 2 * real_b;
+    bool in_real = adjoint ? cfg.type == BBFFT_C2R : cfg.type == BBFFT_R2C;
+    bool out_real = adjoint ? cfg.type == BBFFT_R2C : cfg.type == BBFFT_C2R;
+    std::size_t const *ist = adjoint ? cfg.ostride : cfg.istride;
+    std::size_t const *ost = adjoint ? cfg.istride : cfg.ostride;
+    std::size_t isize = ist[dim + 1] * cfg.shape[dim + 1] * (in_real ? real_b : cplx_b);
+    std::size_t osize = ost[dim + 1] * cfg.shape[dim + 1] * (out_real ? real_b : cplx_b);
+    if (isize > osize) {
+        plan.tmp = std::make_shared<device_buffer>(isize);
+    }
+    std::size_t n = plan.passes.size();
+    for (std::size_t i = 0; i < n; ++i) {
+        plan.passes[i].in_sel = i == 0 ? 0 : 2;
+        plan.passes[i].out_sel = i + 1 == n ? 1 : 2;
+    }
+    plan.inplace_ok = true;
+    for (auto const &ps : plan.passes) {
+        plan.inplace_ok = plan.inplace_ok && ps.inplace_ok;
+    }
+}
+
+static void execute_impl(bbfft_plan_s &plan, const void *in, void *out, cudaStream_t stream) {
+    if (in == out && !plan.inplace_ok) {
+        bad_config("The plan does not support in-place transform on the current device. Please "
+                   "use the out-of-place transform.");
+    }
+    int cur = -1;
+    GB_CUDA(cudaGetDevice(&cur));
+    if (cur != plan.device) {
+        GB_CUDA(cudaSetDevice(plan.device));
+    }
+    void *tmp = plan.tmp ? plan.tmp->ptr : out;
+    for (auto &ps : plan.passes) {
+        fft_params p = ps.p;
+        p.in = ps.in_sel == 0 ? in : tmp;
+        p.out = ps.out_sel == 1 ? out : tmp;
+        void *args[] = {&p};
+        cudaError_t e = cudaLaunchKernel(ps.func, dim3(ps.grid), dim3(ps.block), args, ps.smem, stream);
+        if (e != cudaSuccess) {
+            if (cur != plan.device) {
+                cudaSetDevice(cur);
+            }
+            throw status_error(BBFFT_CUDA_ERROR,
+                               std::string("kernel launch failed: ") + cudaGetErrorString(e));
+        }
+    }
+    if (cur != plan.device) {
+        GB_CUDA(cudaSetDevice(cur));
+    }
+}
+
+} // namespace gbfft
+
+// ------------------------------------------------------------------------------------------
+// C ABI
+
+using gbfft::guarded;
+using gbfft::status_error;
+
+extern "C" {
+
+const char *bbfft_last_error(void) { return gbfft::tl_error.c_str(); }
+const char *bbfft_version(void) { return "bbfft-gb300 0.1.0 (sm_103a)"; }
+
+int bbfft_default_istride(uint32_t dim, const size_t shape[BBFFT_MAX_TENSOR_DIM], int32_t type,
+                          int inplace, size_t stride_out[BBFFT_MAX_TENSOR_DIM]) {
+    return guarded([&] {
+        if (!shape || !stride_out) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "null pointer");
+        }
+        gbfft::from_array(gbfft::default_istride(dim, gbfft::to_array(shape), type, inplace != 0),
+                          stride_out);
+    });
+}
+
+int bbfft_default_ostride(uint32_t dim, const size_t shape[BBFFT_MAX_TENSOR_DIM], int32_t type,
+                          int inplace, size_t stride_out[BBFFT_MAX_TENSOR_DIM]) {
+    return guarded([&] {
+        if (!shape || !stride_out) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "null pointer");
+        }
+        gbfft::from_array(gbfft::default_ostride(dim, gbfft::to_array(shape), type, inplace != 0),
+                          stride_out);
+    });
+}
+
+static void copy_string(std::string const &s, char *buf, size_t buf_len, size_t *needed) {
+    if (needed) {
+        *needed = s.size() + 1;
+    }
+    if (buf && buf_len) {
+        size_t n = std::min(buf_len - 1, s.size());
+        std::memcpy(buf, s.data(), n);
+        buf[n] = '\0';
+    }
+}
+
+int bbfft_configuration_to_string(const bbfft_configuration *cfg, char *buf, size_t buf_len,
+                                  size_t *needed) {
+    return guarded([&] {
+        if (!cfg) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "null configuration");
+        }
+        copy_string(gbfft::to_descriptor(*cfg), buf, buf_len, needed);
+    });
+}
+
+int bbfft_parse_fft_descriptor(const char *desc, bbfft_configuration *cfg) {
+    return guarded([&] {
+        if (!desc || !cfg) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "null pointer");
+        }
+        *cfg = gbfft::parse_descriptor(desc);
+    });
+}
+
+int bbfft_jit_cache_create(bbfft_cache_t *cache) {
+    return guarded([&] {
+        if (!cache) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "null pointer");
+        }
+        *cache = new bbfft_cache_s();
+    });
+}
+
+int bbfft_aot_cache_create(bbfft_cache_t *cache) {
+    return guarded([&] {
+        if (!cache) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "null pointer");
+        }
+        auto c = new bbfft_cache_s();
+        c->aot = true;
+        *cache = c;
+    });
+}
+
+int bbfft_aot_cache_register_module(bbfft_cache_t cache, const void *image, size_t image_size,
+                                    const char *const *kernel_names, size_t num_kernel_names,
+                                    int device) {
+    return guarded([&] {
+        if (!cache || !cache->aot || !image || image_size == 0) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "invalid aot module registration");
+        }
+        int cur = 0;
+        GB_CUDA(cudaGetDevice(&cur));
+        if (cur != device) {
+            GB_CUDA(cudaSetDevice(device));
+        }
+        auto m = std::make_shared<gbfft::module>();
+        cudaError_t e =
+            cudaLibraryLoadData(&m->lib, image, nullptr, nullptr, 0, nullptr, nullptr, 0);
+        if (cur != device) {
+            cudaSetDevice(cur);
+        }
+        if (e != cudaSuccess) {
+            throw status_error(BBFFT_CUDA_ERROR,
+                               std::string("cudaLibraryLoadData failed: ") + cudaGetErrorString(e));
+        }
+        bbfft_cache_s::aot_module am;
+        am.mod = m;
+        am.device = device;
+        for (size_t i = 0; i < num_kernel_names; ++i) {
+            am.names.insert(kernel_names[i]);
+        }
+        std::lock_guard<std::mutex> lock(cache->mu);
+        cache->aot_modules.push_back(std::move(am));
+    });
+}
+
+int bbfft_cache_destroy(bbfft_cache_t cache) {
+    return guarded([&] { delete cache; });
+}
+
+int bbfft_cache_kernel_names(bbfft_cache_t cache, char *buf, size_t buf_len, size_t *needed) {
+    return guarded([&] {
+        if (!cache) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "null cache");
+        }
+        std::string s;
+        std::lock_guard<std::mutex> lock(cache->mu);
+        std::vector<std::string> names;
+        if (cache->aot) {
+            for (auto const &m : cache->aot_modules) {
+                names.insert(names.end(), m.names.begin(), m.names.end());
+            }
+        } else {
+            for (auto const &kv : cache->jit) {
+                names.push_back(kv.first.substr(0, kv.first.rfind('@')));
+            }
+        }
+        std::sort(names.begin(), names.end());
+        for (auto const &n : names) {
+            s += n + "\n";
+        }
+        copy_string(s, buf, buf_len, needed);
+    });
+}
+
+int bbfft_cache_stats(bbfft_cache_t cache, uint64_t *hits, uint64_t *misses) {
+    return guarded([&] {
+        if (!cache) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "null cache");
+        }
+        if (hits) {
+            *hits = cache->hits.load();
+        }
+        if (misses) {
+            *misses = cache->misses.load();
+        }
+    });
+}
+
+static int create_common(const bbfft_configuration *cfg, cudaStream_t stream, bbfft_cache_t cache,
+                         bool adjoint, bbfft_plan_t *plan, gbfft::pass_request const *tuning) {
+    return guarded([&] {
+        if (!cfg || !plan) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "null pointer");
+        }
+        *plan = nullptr;
+        std::unique_ptr<bbfft_plan_s> p(new bbfft_plan_s());
+        gbfft::make_plan_impl(*cfg, stream, cache, adjoint, *p, tuning);
+        *plan = p.release();
+    });
+}
+
+int bbfft_plan_create(const bbfft_configuration *cfg, cudaStream_t stream, bbfft_cache_t cache,
+                      bbfft_plan_t *plan) {
+    return create_common(cfg, stream, cache, false, plan, nullptr);
+}
+
+int bbfft_plan_create_adjoint(const bbfft_configuration *cfg, cudaStream_t stream,
+                              bbfft_cache_t cache, bbfft_plan_t *plan) {
+    return create_common(cfg, stream, cache, true, plan, nullptr);
+}
+
+int bbfft_plan_create_tuned(const bbfft_configuration *cfg, cudaStream_t stream,
+                            const uint32_t *radices, uint32_t num_radices,
+                            uint32_t threads_per_transform, uint32_t mb, uint32_t kb,
+                            bbfft_plan_t *plan) {
+    gbfft::pass_request t{};
+    if (radices) {
+        for (uint32_t i = 0; i < num_radices && radices[i] != 0; ++i) {
+            t.radices.push_back(static_cast<int>(radices[i]));
+        }
+    }
+    t.T = static_cast<int>(threads_per_transform);
+    t.Mb = static_cast<int>(mb);
+    t.Kb = static_cast<int>(kb);
+    if (cfg && cfg->dim != 1) {
+        gbfft::tl_error = "tuned plans are 1d only";
+        return BBFFT_BAD_CONFIGURATION;
+    }
+    return create_common(cfg, stream, nullptr, false, plan, &t);
+}
+
+int bbfft_plan_execute(bbfft_plan_t plan, const void *in, void *out, uint32_t num_wait_events,
+                       const cudaEvent_t *wait_events, cudaEvent_t signal_event) {
+    return guarded([&] {
+        if (!plan) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "null plan");
+        }
+        if (num_wait_events && !wait_events) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "num_wait_events > 0 but no events");
+        }
+        for (uint32_t i = 0; i < num_wait_events; ++i) {
+            GB_CUDA(cudaStreamWaitEvent(plan->stream, wait_events[i], 0));
+        }
+        gbfft::execute_impl(*plan, in, out, plan->stream);
+        if (signal_event) {
+            GB_CUDA(cudaEventRecord(signal_event, plan->stream));
+        }
+    });
+}
+
+int bbfft_plan_execute_on(bbfft_plan_t plan, const void *in, void *out, cudaStream_t stream) {
+    return guarded([&] {
+        if (!plan) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "null plan");
+        }
+        gbfft::execute_impl(*plan, in, out, stream);
+    });
+}
+
+int bbfft_plan_retain(bbfft_plan_t plan) {
+    return guarded([&] {
+        if (!plan) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "null plan");
+        }
+        plan->refs++;
+    });
+}
+
+int bbfft_plan_destroy(bbfft_plan_t plan) {
+    return guarded([&] {
+        if (plan && --plan->refs == 0) {
+            delete plan;
+        }
+    });
+}
+
+int bbfft_plan_get_info(bbfft_plan_t plan, bbfft_plan_info *info) {
+    return guarded([&] {
+        if (!plan || !info) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "null pointer");
+        }
+        std::memset(info, 0, sizeof(*info));
+        auto const &ps = plan->passes.front();
+        std::strncpy(info->identifier, ps.identifier.c_str(), sizeof(info->identifier) - 1);
+        info->num_launches = static_cast<uint32_t>(plan->passes.size());
+        info->inplace_supported = plan->inplace_ok;
+        info->jit_compiled = plan->jit;
+        info->num_stages = static_cast<uint32_t>(ps.p.L);
+        for (int s = 0; s < ps.p.L && s < 12; ++s) {
+            info->radix[s] = static_cast<uint32_t>(ps.p.radix[s]);
+        }
+        info->threads_per_transform = static_cast<uint32_t>(ps.p.T);
+        info->mb = static_cast<uint32_t>(ps.p.Mb);
+        info->kb = static_cast<uint32_t>(ps.p.Kb);
+        info->block_threads = ps.block;
+        info->shared_bytes = ps.smem;
+        info->workspace_bytes = plan->tmp ? plan->tmp->bytes : 0;
+    });
+}
+
+} // extern "C"

@@ -1,0 +1,48 @@
+// Kernel parameter block shared by the host library and the device engine.
+// Plain C++ (no CUDA types) so that the host compiler, nvcc and NVRTC agree on the layout.
+#pragma once
+
+namespace gbfft {
+
+constexpr int max_stages = 12;
+
+enum kind : int {
+    kind_c2c = 0,
+    kind_r2c_half = 1, // even N
+    kind_r2c_full = 2, // odd N
+    kind_c2r_half = 3, // even N
+    kind_c2r_full = 4, // odd N
+};
+
+
+// flags
+constexpr int flag_conj_in = 1;       // c2c: conjugate on load (backward)
+constexpr int flag_conj_out = 2;      // c2c: conjugate on store (backward)
+constexpr int flag_adj_r2c = 4;       // adjoint of r2c, run as a c2r kernel (Hermitian weights)
+constexpr int flag_adj_c2r = 8;       // adjoint of c2r, run as a r2c kernel (Hermitian weights)
+constexpr int flag_scale_out = 16;    // multiply the output by params.scale
+
+
+struct fft_params {
+    const void *in;
+    void *out;
+    const void *tw;        // w_Nt^{-i}, i = 0..Nt-1, complex of the plan precision
+    long long M;           // left batch
+    long long K;           // right batch
+    long long is1, is2;    // input strides of the N and K mode (elements)
+    long long os1, os2;    // output strides of the N and K mode (elements)
+    int N;                 // logical FFT length
+    int Nc;                // complex FFT length (N or N/2)
+    int Nt;                // twiddle table length
+    int L;                 // number of stages
+    int radix[max_stages]; // radix per stage; 1 = copy stage
+    int T;                 // threads per transform
+    int Mb, Kb;            // tile
+    int m_tiles;           // ceil(M / Mb)
+    int flags;
+    int nbuf;              // shared buffers (1 or 2)
+    int buf_elems;         // padded elements per buffer
+    double scale;          // used with flag_scale_out
+};
+
+} // namespace gbfft

@@ -1,0 +1,203 @@
+/*
+ * bbfft_gb300.h - C ABI of the GB300 (sm_103a) double-batched FFT library.
+ *
+ * This is the drop-in boundary for the hot path of Intel's double-batched FFT
+ * library (bbfft 0.5.1): many small FFTs over an M x N1..Nd x K tensor.  Every
+ * entry point names the reference interface it replaces.  The C++ API of the
+ * reference (bbfft::configuration, bbfft::make_plan, bbfft::plan<E>::execute, the
+ * jit/aot caches) is provided header-only on top of this ABI in include/bbfft/.
+ *
+ * Conventions
+ *  - Functions return BBFFT_SUCCESS (0) or a negative status; the message of the last
+ *    failure on the calling thread is returned by bbfft_last_error().
+ *  - Pointers to tensors are device pointers (cudaMalloc'd or managed).  Offsets and
+ *    strides are counted in elements: real elements for real tensors, complex
+ *    elements for complex tensors (reference include/bbfft/configuration.hpp:162-179).
+ *  - Streams and events are the CUDA runtime's cudaStream_t / cudaEvent_t; a null
+ *    stream is the legacy default stream.
+ *  - No entry point synchronises the device unless stated.
+ */
+#ifndef BBFFT_GB300_H
+#define BBFFT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include <cuda_runtime_api.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define BBFFT_GB300_API __declspec(dllexport)
+#else
+#define BBFFT_GB300_API __attribute__((visibility("default")))
+#endif
+
+/* ---- status codes (reference: exceptions bad_configuration / cl::error / ze::error /
+ *      std::runtime_error, include/bbfft/bad_configuration.hpp:17-40) ---- */
+typedef enum bbfft_status {
+    BBFFT_SUCCESS = 0,
+    BBFFT_BAD_CONFIGURATION = -1, /* bbfft::bad_configuration */
+    BBFFT_INVALID_ARGUMENT = -2,  /* null pointers, bad sizes */
+    BBFFT_CUDA_ERROR = -3,        /* a CUDA runtime call failed */
+    BBFFT_COMPILE_ERROR = -4,     /* NVRTC could not compile user callbacks */
+    BBFFT_PARSE_ERROR = -5,       /* malformed descriptor (std::runtime_error in the reference) */
+    BBFFT_OUT_OF_MEMORY = -6,
+    BBFFT_INTERNAL_ERROR = -7,
+    BBFFT_DEVICE_ERROR = -8 /* a kernel reported an error status (e.g. a bounded wait ran out) */
+} bbfft_status;
+
+#define BBFFT_MAX_FFT_DIM 3
+#define BBFFT_MAX_TENSOR_DIM 5
+
+/* reference: enum class precision (configuration.hpp:22-25): value = bytes per real */
+#define BBFFT_PRECISION_F32 4
+#define BBFFT_PRECISION_F64 8
+/* reference: enum class direction (configuration.hpp:67-70) */
+#define BBFFT_FORWARD (-1)
+#define BBFFT_BACKWARD 1
+/* reference: enum class transform_type (configuration.hpp:79-83) */
+#define BBFFT_C2C 0
+#define BBFFT_R2C 1
+#define BBFFT_C2R 2
+
+/* Arithmetic used by the DFT stages (no counterpart in the reference, which computes in
+ * the plan precision only).  F32 plans only; F64 plans always use BBFFT_COMPUTE_NATIVE. */
+#define BBFFT_COMPUTE_NATIVE 0    /* plain FP32 / FP64 on CUDA cores */
+#define BBFFT_COMPUTE_BF16 1      /* tensor-core DFT stages, BF16 operands, FP32 accumulate */
+#define BBFFT_COMPUTE_SPLIT_BF16 2 /* tensor-core DFT stages, 3-term split-BF16 products */
+
+/*
+ * FFT configuration; mirrors bbfft::configuration (reference
+ * include/bbfft/configuration.hpp:151-192) and bbfft::user_module
+ * (include/bbfft/user_module.hpp:24-37).  Callbacks are CUDA C++ source defining
+ *   T load(const T* in, size_t offset)          -- T = float2/double2 or float/double
+ *   void store(T* out, size_t offset, T value)
+ * compiled for sm_103a with NVRTC at plan creation (the reference compiles OpenCL-C).
+ */
+typedef struct bbfft_configuration {
+    uint32_t dim;                             /* 1..3 */
+    size_t shape[BBFFT_MAX_TENSOR_DIM];       /* {M, N1, .., Nd, K} */
+    int32_t precision;                        /* BBFFT_PRECISION_F32 / _F64 */
+    int32_t direction;                        /* BBFFT_FORWARD / BBFFT_BACKWARD */
+    int32_t type;                             /* BBFFT_C2C / _R2C / _C2R */
+    size_t istride[BBFFT_MAX_TENSOR_DIM];     /* s0..s_{d+1}; s0 must be 1 */
+    size_t ostride[BBFFT_MAX_TENSOR_DIM];
+    const char *callback_source;              /* user_module::data (may be NULL) */
+    size_t callback_length;                   /* user_module::length */
+    const char *load_function;                /* user_module::load_function (may be NULL) */
+    const char *store_function;               /* user_module::store_function (may be NULL) */
+    int32_t compute;                          /* BBFFT_COMPUTE_*; 0 for the reference behaviour */
+} bbfft_configuration;
+
+typedef struct bbfft_plan_s *bbfft_plan_t;
+typedef struct bbfft_cache_s *bbfft_cache_t;
+
+/* ---- configuration helpers ---- */
+
+/* reference: default_istride (src/base/configuration.cpp:24-43) */
+BBFFT_GB300_API int bbfft_default_istride(uint32_t dim, const size_t shape[BBFFT_MAX_TENSOR_DIM],
+                                          int32_t type, int inplace,
+                                          size_t stride_out[BBFFT_MAX_TENSOR_DIM]);
+/* reference: default_ostride (src/base/configuration.cpp:45-56) */
+BBFFT_GB300_API int bbfft_default_ostride(uint32_t dim, const size_t shape[BBFFT_MAX_TENSOR_DIM],
+                                          int32_t type, int inplace,
+                                          size_t stride_out[BBFFT_MAX_TENSOR_DIM]);
+/* reference: configuration::to_string / operator<< (src/base/configuration.cpp:63-160).
+ * Writes at most buf_len bytes including the terminating zero; *needed receives the full
+ * length + 1 (may be NULL). */
+BBFFT_GB300_API int bbfft_configuration_to_string(const bbfft_configuration *cfg, char *buf,
+                                                  size_t buf_len, size_t *needed);
+/* reference: parse_fft_descriptor (src/base/parser.cpp:59-211) */
+BBFFT_GB300_API int bbfft_parse_fft_descriptor(const char *desc, bbfft_configuration *cfg);
+
+/* ---- caches (reference include/bbfft/jit_cache.hpp:23-69, jit_cache_all.hpp:20-37,
+ *      aot_cache.hpp:21-48) ---- */
+
+/* reference: jit_cache_all (src/base/jit_cache_all.cpp:10-26): stores every module that
+ * plan creation compiles, keyed by (kernel identifier, device id). */
+BBFFT_GB300_API int bbfft_jit_cache_create(bbfft_cache_t *cache);
+/* reference: aot_cache (src/base/aot_cache.cpp:12-28): look-up only; modules are
+ * registered with bbfft_aot_cache_register_module. */
+BBFFT_GB300_API int bbfft_aot_cache_create(bbfft_cache_t *cache);
+/* reference: aot_cache::register_module (src/base/aot_cache.cpp:26-28).  `image` is a
+ * cubin / fatbin for sm_103a holding kernels named by `kernel_names`. */
+BBFFT_GB300_API int bbfft_aot_cache_register_module(bbfft_cache_t cache, const void *image,
+                                                    size_t image_size,
+                                                    const char *const *kernel_names,
+                                                    size_t num_kernel_names, int device);
+BBFFT_GB300_API int bbfft_cache_destroy(bbfft_cache_t cache);
+/* reference: jit_cache_all::kernel_names (jit_cache_all.hpp:33) */
+BBFFT_GB300_API int bbfft_cache_kernel_names(bbfft_cache_t cache, char *buf, size_t buf_len,
+                                             size_t *needed);
+/* number of cache look-ups that hit / missed since creation (no counterpart; test hook) */
+BBFFT_GB300_API int bbfft_cache_stats(bbfft_cache_t cache, uint64_t *hits, uint64_t *misses);
+
+/* ---- plans ---- */
+
+/* reference: make_plan(cfg, queue, cache) (include/bbfft/sycl/make_plan.hpp:27,40;
+ * cl/make_plan.hpp:27,40; ze/make_plan.hpp:29) -> select_fft_algorithm
+ * (src/common/algorithm.hpp:20-30).  The plan is bound to the current CUDA device and to
+ * `stream`; `cache` may be NULL. */
+BBFFT_GB300_API int bbfft_plan_create(const bbfft_configuration *cfg, cudaStream_t stream,
+                                      bbfft_cache_t cache, bbfft_plan_t *plan);
+
+/* Adjoint of the transform described by cfg (no counterpart in the reference): c2c
+ * forward -> unnormalised backward; r2c -> c2r with Hermitian weights (interior bins
+ * halved, imaginary parts of DC and Nyquist dropped); c2r -> r2c with interior bins
+ * doubled.  The plan maps tensors laid out like cfg's OUTPUT to tensors laid out like
+ * cfg's INPUT. */
+BBFFT_GB300_API int bbfft_plan_create_adjoint(const bbfft_configuration *cfg, cudaStream_t stream,
+                                              bbfft_cache_t cache, bbfft_plan_t *plan);
+
+/* reference: plan<E>::execute(in, out, dep_events) (include/bbfft/plan.hpp:77-131) and
+ * plan_unmanaged_event::execute(in, out, signal, n_wait, wait) (plan.hpp:165-183).
+ * Waits on `wait_events` (cudaStreamWaitEvent), launches on the plan's stream and, if
+ * `signal_event` is not NULL, records it after the launch.  in == out is in-place. */
+BBFFT_GB300_API int bbfft_plan_execute(bbfft_plan_t plan, const void *in, void *out,
+                                       uint32_t num_wait_events, const cudaEvent_t *wait_events,
+                                       cudaEvent_t signal_event);
+/* Same, on an explicit stream instead of the plan's stream. */
+BBFFT_GB300_API int bbfft_plan_execute_on(bbfft_plan_t plan, const void *in, void *out,
+                                          cudaStream_t stream);
+/* Copies of plans share the implementation (reference plan.hpp:24-48: shared_ptr). */
+BBFFT_GB300_API int bbfft_plan_retain(bbfft_plan_t plan);
+BBFFT_GB300_API int bbfft_plan_destroy(bbfft_plan_t plan);
+
+/* Plan introspection (no counterpart; the reference exposes the kernel identifier only
+ * through the cache key, src/common/algorithm/small_batch_fft.hpp:64-67). */
+typedef struct bbfft_plan_info {
+    char identifier[256];  /* kernel identifier used as cache key */
+    uint32_t num_launches; /* kernels per execute (d for an nd plan) */
+    uint32_t inplace_supported;
+    uint32_t jit_compiled; /* 1 if a kernel of this plan came from NVRTC or the cache */
+    uint32_t radix[12];    /* radices of the first pass */
+    uint32_t num_stages;
+    uint32_t threads_per_transform;
+    uint32_t mb, kb;        /* tile of the first pass */
+    uint32_t block_threads; /* threads per CTA of the first pass */
+    size_t shared_bytes;    /* dynamic shared memory of the first pass */
+    size_t workspace_bytes; /* device scratch owned by the plan (nd temporaries) */
+} bbfft_plan_info;
+BBFFT_GB300_API int bbfft_plan_get_info(bbfft_plan_t plan, bbfft_plan_info *info);
+
+/* Override the automatic blocking of a 1d plan (autotuner hook; no counterpart).
+ * radices: list of radices whose product is the complex FFT length; 0-terminated or
+ * num_radices long.  threads_per_transform, mb, kb: 0 = automatic. */
+BBFFT_GB300_API int bbfft_plan_create_tuned(const bbfft_configuration *cfg, cudaStream_t stream,
+                                            const uint32_t *radices, uint32_t num_radices,
+                                            uint32_t threads_per_transform, uint32_t mb,
+                                            uint32_t kb, bbfft_plan_t *plan);
+
+/* Thread-local message of the last failure (empty string if none). */
+BBFFT_GB300_API const char *bbfft_last_error(void);
+/* Library version string. */
+BBFFT_GB300_API const char *bbfft_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BBFFT_GB300_H */

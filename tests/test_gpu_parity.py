@@ -1,0 +1,259 @@
+"""GPU parity of the 1d and nd plans with the reference's own device tests and the oracle.
+
+Known-answer cases restate test/c2c.cpp, test/r2c.cpp (1d..3d) of the reference; random
+cases compare with the C restatement of the reference algorithm in FP64 (oracle/) and
+require rel-L2 <= 2e-6 (float) / 1e-14 (double) as the benchmark spec's tolerances state.
+The element-wise check uses the reference's tolerance tol(N) = 100 eps sqrt(N)
+(test/fft.hpp:17-20) with doctest's Approx semantics |a-b| < tol (1 + max(|a|,|b|))."""
+import numpy as np
+import pytest
+
+from gpu_helpers import TOL, dtypes, rel_l2, run
+
+pytestmark = pytest.mark.gpu
+
+PRECS = [4, 8]
+
+
+def approx_ok(a, ref, eps):
+    a = np.asarray(a)
+    ref = np.asarray(ref)
+    for part in (np.real, np.imag):
+        x, r = part(a).astype(np.float64), part(ref).astype(np.float64)
+        bound = eps * (1.0 + np.maximum(np.abs(x), np.abs(r)))
+        if not np.all(np.abs(x - r) < bound):
+            i = np.argmax(np.abs(x - r) - bound)
+            return False, (i, x.ravel()[i], r.ravel()[i])
+    return True, None
+
+
+def tol(prec, N):
+    eps = np.finfo(np.float32 if prec == 4 else np.float64).eps
+    return 100.0 * eps * np.sqrt(N)
+
+
+# ---------------------------------------------------------------- c2c (test/c2c.cpp)
+
+C2C_M = [1, 2, 3, 16, 17, 64, 256, 1024]
+C2C_N = [2, 3, 5, 7, 11, 13, 4, 8, 16, 32, 128, 256, 512, 27, 63, 105, 363]
+
+
+@pytest.mark.parametrize('prec', PRECS)
+@pytest.mark.parametrize('K', [1, 32])
+@pytest.mark.parametrize('N', C2C_N)
+def test_c2c_forward_known_answer(bb, po, torch_cuda, prec, K, N):
+    """reference test/c2c.cpp:53-66 (in-place, default layout)"""
+    torch = torch_cuda
+    for M in C2C_M:
+        x, X = po.c2c_known_answer(M, N, K, prec)
+        cfg = bb.configuration(1, [M, N, K], precision=prec)
+        out = run(bb, torch, cfg, x.ravel(), x.size, dtypes(prec)[1], inplace=True)
+        ok, where = approx_ok(out.reshape(K, N, M), X, tol(prec, N))
+        assert ok, (M, N, K, where)
+
+
+@pytest.mark.parametrize('prec', PRECS)
+@pytest.mark.parametrize('N', [6, 17, 102])
+@pytest.mark.parametrize('M', [1, 32])
+def test_c2c_non_packed(bb, po, torch_cuda, prec, N, M):
+    """reference test/c2c.cpp:68-82: stride {1, M+1, (M+1)(N+1)}, K = 33"""
+    torch = torch_cuda
+    K = 33
+    stride = [1, M + 1, (M + 1) * (N + 1), 0, 0]
+    x, X = po.c2c_known_answer(M, N, K, prec)
+    size = po.tensor_size(1, [M, N, K], stride)
+    xf = po.scatter(x, 1, [M, N, K], stride, size, dtypes(prec)[1])
+    cfg = bb.configuration(1, [M, N, K], precision=prec, istride=stride, ostride=stride)
+    out = run(bb, torch, cfg, xf, size, dtypes(prec)[1], inplace=True)
+    ok, where = approx_ok(po.gather(out, 1, [M, N, K], stride), X, tol(prec, N))
+    assert ok, where
+
+
+@pytest.mark.parametrize('prec', PRECS)
+@pytest.mark.parametrize('N', [5, 63, 92])
+@pytest.mark.parametrize('M', [1, 32])
+def test_c2c_identity(bb, torch_cuda, prec, N, M):
+    """reference test/c2c.cpp:84-127: backward(forward(x)) / N == x"""
+    torch = torch_cuda
+    K = 16
+    rng = np.random.default_rng(1000 + N + M)
+    x = (rng.uniform(0, 1, M * N * K) + 1j * rng.uniform(0, 1, M * N * K)).astype(dtypes(prec)[1])
+    f = bb.configuration(1, [M, N, K], precision=prec, direction=bb.FORWARD)
+    b = bb.configuration(1, [M, N, K], precision=prec, direction=bb.BACKWARD)
+    y = run(bb, torch, f, x, x.size, dtypes(prec)[1], inplace=True)
+    z = run(bb, torch, b, y, x.size, dtypes(prec)[1], inplace=True)
+    ok, where = approx_ok(x, z / N, tol(prec, N))
+    assert ok, where
+
+
+# ---------------------------------------------------------------- r2c / c2r (test/r2c.cpp)
+
+def _r2c_case(bb, po, torch, prec, M, Ns, K, inplace):
+    dim = len(Ns)
+    shape = [M] + list(Ns) + [K]
+    cfg = bb.configuration(dim, shape, precision=prec, type=bb.R2C, inplace=inplace)
+    ist, ost = list(cfg.istride), list(cfg.ostride)
+    x, X = po.r2c_known_answer(M, Ns, K, prec)
+    ishape = list(shape)
+    if inplace:
+        ishape[1] = 2 * (Ns[0] // 2 + 1)
+    xs = np.zeros([K] + ([ishape[d + 1] for d in range(dim)][::-1]) + [M], dtype=x.dtype)
+    xs[tuple([slice(None)] * dim + [slice(0, Ns[0])] + [slice(None)])] = x
+    isize = po.tensor_size(dim, ishape, ist)
+    xf = po.scatter(xs, dim, ishape, ist, isize, dtypes(prec)[0])
+    oshape = list(shape)
+    oshape[1] = Ns[0] // 2 + 1
+    osize = po.tensor_size(dim, oshape, ost)
+    out = run(bb, torch, cfg, xf, osize, dtypes(prec)[1], inplace=inplace)
+    got = po.gather(out, dim, oshape, ost)
+    ok, where = approx_ok(got, X, tol(prec, int(np.prod(Ns))))
+    assert ok, (M, Ns, K, inplace, where)
+
+
+def _c2r_case(bb, po, torch, prec, M, Ns, K, inplace, pollute=False):
+    dim = len(Ns)
+    shape = [M] + list(Ns) + [K]
+    cfg = bb.configuration(dim, shape, precision=prec, type=bb.C2R, direction=bb.BACKWARD,
+                           inplace=inplace)
+    ist, ost = list(cfg.istride), list(cfg.ostride)
+    X, y = po.c2r_known_answer(M, Ns, K, prec, pollute_0=pollute)
+    ishape = list(shape)
+    ishape[1] = Ns[0] // 2 + 1
+    isize = po.tensor_size(dim, ishape, ist)
+    Xf = po.scatter(X, dim, ishape, ist, isize, dtypes(prec)[1])
+    oshape = list(shape)
+    if inplace:
+        oshape[1] = 2 * (Ns[0] // 2 + 1)
+    osize = po.tensor_size(dim, oshape, ost)
+    out = run(bb, torch, cfg, Xf, osize, dtypes(prec)[0], inplace=inplace)
+    got = po.gather(out, dim, oshape, ost)
+    got = got[tuple([slice(None)] * dim + [slice(0, Ns[0])] + [slice(None)])]
+    ok, where = approx_ok(got, y, tol(prec, int(np.prod(Ns))))
+    assert ok, (M, Ns, K, inplace, where)
+
+
+@pytest.mark.parametrize('prec', PRECS)
+@pytest.mark.parametrize('N', [2, 4, 5, 8, 27, 16, 32, 128, 105, 256, 512, 102, 220, 10, 26])
+def test_r2c_1d_out_of_place(bb, po, torch_cuda, prec, N):
+    """reference test/r2c.cpp:182-192"""
+    for K in (1, 33):
+        for M in (1, 3, 32):
+            _r2c_case(bb, po, torch_cuda, prec, M, [N], K, False)
+
+
+@pytest.mark.parametrize('prec', PRECS)
+@pytest.mark.parametrize('N', [4, 12, 13, 110])
+def test_r2c_1d_in_place(bb, po, torch_cuda, prec, N):
+    """reference test/r2c.cpp:194-203"""
+    for M in (1, 3):
+        _r2c_case(bb, po, torch_cuda, prec, M, [N], 65, True)
+
+
+@pytest.mark.parametrize('prec', PRECS)
+@pytest.mark.parametrize('Ns,inplace', [((4, 8), True), ((8, 5), True), ((5, 4), False),
+                                        ((10, 3), False), ((4, 8, 2), True), ((8, 256, 5), True),
+                                        ((5, 4, 6), False), ((10, 286, 3), False)])
+def test_r2c_nd(bb, po, torch_cuda, prec, Ns, inplace):
+    """reference test/r2c.cpp:205-250"""
+    for K in (1, 33) if inplace else (1, 65):
+        for M in (1, 3) if inplace else (1, 7):
+            _r2c_case(bb, po, torch_cuda, prec, M, list(Ns), K, inplace)
+
+
+@pytest.mark.parametrize('prec', PRECS)
+@pytest.mark.parametrize('N', [11, 16, 25, 96, 256, 300, 315])
+def test_c2r_1d_out_of_place(bb, po, torch_cuda, prec, N):
+    """reference test/r2c.cpp:299-308"""
+    for M in (1, 5, 32):
+        _c2r_case(bb, po, torch_cuda, prec, M, [N], 33, False)
+
+
+@pytest.mark.parametrize('prec', PRECS)
+@pytest.mark.parametrize('N', [5, 16, 21, 48, 512])
+def test_c2r_1d_in_place_polluted_0(bb, po, torch_cuda, prec, N):
+    """reference test/r2c.cpp:310-324: imag(X[0]) must be ignored"""
+    _c2r_case(bb, po, torch_cuda, prec, 1, [N], 33, True, pollute=True)
+
+
+@pytest.mark.parametrize('prec', PRECS)
+@pytest.mark.parametrize('Ns,inplace', [((4, 2), True), ((96, 96), True), ((4, 8, 2), True),
+                                        ((96, 96, 80), True), ((5, 4), False), ((10, 3), False),
+                                        ((5, 4, 6), False), ((10, 286, 3), False)])
+def test_c2r_nd(bb, po, torch_cuda, prec, Ns, inplace):
+    """reference test/r2c.cpp:326-372"""
+    for K in ((1, 54) if inplace else (1, 65)):
+        for M in ((1, 3) if inplace else (1, 7)):
+            if np.prod(Ns) * K * M > 4_000_000:
+                continue  # keep the largest 3d case at K=1/M=1..3 within test time
+            _c2r_case(bb, po, torch_cuda, prec, M, list(Ns), K, inplace)
+
+
+@pytest.mark.parametrize('prec', PRECS)
+@pytest.mark.parametrize('Ns,K,M,inplace', [((8,), 16, 1, True), ((64,), 16, 8, True),
+                                             ((212,), 16, 8, True), ((8,), 16, 1, False),
+                                             ((64,), 16, 8, False), ((212,), 16, 1, False),
+                                             ((8, 8, 8), 11, 7, True), ((96, 96, 80), 1, 1, True)])
+def test_real_identity(bb, po, torch_cuda, prec, Ns, K, M, inplace):
+    """reference test/r2c.cpp:376-497: c2r(r2c(x)) / prod(N) == x"""
+    torch = torch_cuda
+    dim = len(Ns)
+    shape = [M] + list(Ns) + [K]
+    f = bb.configuration(dim, shape, precision=prec, type=bb.R2C, inplace=inplace)
+    b = bb.configuration(dim, shape, precision=prec, type=bb.C2R, direction=bb.BACKWARD,
+                         inplace=inplace)
+    rng = np.random.default_rng(7 + sum(Ns) + K + M)
+    ishape = list(shape)
+    if inplace:
+        ishape[1] = 2 * (Ns[0] // 2 + 1)
+    isize = po.tensor_size(dim, ishape, list(f.istride))
+    x = rng.uniform(0, 1, isize).astype(dtypes(prec)[0])
+    oshape = list(shape)
+    oshape[1] = Ns[0] // 2 + 1
+    osize = po.tensor_size(dim, oshape, list(f.ostride))
+    X = run(bb, torch, f, x, osize if not inplace else osize, dtypes(prec)[1], inplace=inplace)
+    if inplace:
+        y = run(bb, torch, b, X, isize, dtypes(prec)[0], inplace=True)
+    else:
+        y = run(bb, torch, b, X, isize, dtypes(prec)[0])
+    xd = po.gather(x, dim, shape, list(f.istride))
+    yd = po.gather(y, dim, shape, list(b.ostride))
+    ok, where = approx_ok(xd, yd / np.prod(Ns), tol(prec, int(np.prod(Ns))))
+    assert ok, where
+
+
+# ---------------------------------------------------------------- random vs oracle
+
+RANDOM_N = list(range(1, 65)) + [72, 81, 96, 100, 121, 128, 136, 160, 169, 192, 224, 243, 256,
+                                 289, 320, 361, 384, 400, 472, 480, 488, 500, 509, 512]
+
+
+@pytest.mark.parametrize('prec', PRECS)
+@pytest.mark.parametrize('type', [0, 1, 2])
+def test_random_vs_oracle(bb, po, torch_cuda, prec, type):
+    """Every N in 1..64 and a spread of larger N (primes, prime powers, the ragged set),
+    random double batching, against the oracle in FP64: rel-L2 within the north-star
+    tolerance."""
+    torch = torch_cuda
+    rng = np.random.default_rng(42 + type + prec)
+    rdt, cdt = dtypes(prec)
+    worst = 0.0
+    for N in RANDOM_N:
+        if type != 0 and N == 1:
+            continue
+        M = int(rng.choice([1, 2, 5, 8, 33]))
+        K = int(rng.integers(1, 40))
+        for direction in ([bb.FORWARD, bb.BACKWARD] if type == 0 else [None]):
+            d = direction if type == 0 else (bb.FORWARD if type == 1 else bb.BACKWARD)
+            cfg = bb.configuration(1, [M, N, K], precision=prec, type=type, direction=d)
+            nin = N // 2 + 1 if type == 2 else N
+            nout = N // 2 + 1 if type == 1 else N
+            if type == 1:
+                x = rng.standard_normal(M * nin * K).astype(rdt)
+            else:
+                x = (rng.standard_normal(M * nin * K) + 1j * rng.standard_normal(M * nin * K)).astype(cdt)
+            out = run(bb, torch, cfg, x, M * nout * K, rdt if type == 2 else cdt)
+            ref = po.oracle_fft(1, [M, N, K], type, d, x.astype(np.complex128 if type != 1 else np.float64), prec=8)
+            e = rel_l2(out, ref)
+            worst = max(worst, e)
+            assert e <= TOL[prec], (N, M, K, direction, e)
+    print('worst rel-L2', worst)
