@@ -366,6 +366,21 @@ static int max_optin_smem(int device) {
     return v;
 }
 
+// The dynamic shared-memory limit is a property of the kernel, shared by every plan that
+// launches it: raise it once per kernel and device to the device maximum (lowering it for
+// one plan would break the launches of another).
+static void allow_max_smem(const void *func, int device) {
+    static std::mutex mu;
+    static std::set<std::pair<const void *, int>> done;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done.count({func, device})) {
+        return;
+    }
+    GB_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 max_optin_smem(device)));
+    done.insert({func, device});
+}
+
 static std::string c_ident(std::string s) {
     for (auto &ch : s) {
         if (!std::isalnum(static_cast<unsigned char>(ch)) && ch != '_') {
@@ -515,6 +530,11 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     while (Kb > 1 && nbuf * buf_elems(Kb) * celem > soft_limit) {
         Kb /= 2;
     }
+    // a tile of Mb transforms that does not fit is split along M (in-place real
+    // transforms then become unsupported, as in the reference when Mb < M)
+    while (Mb > 1 && nbuf * buf_elems(Kb) * celem > soft_limit) {
+        Mb = (Mb + 1) / 2;
+    }
     std::size_t smem = nbuf * buf_elems(Kb) * celem;
     if (smem > static_cast<std::size_t>(max_optin_smem(device))) {
         bad_config("FFT length " + std::to_string(N) + " needs " + std::to_string(smem) +
@@ -629,8 +649,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         ps.func = reinterpret_cast<const void *>(k);
     }
     if (smem > 48 * 1024) {
-        GB_CUDA(cudaFuncSetAttribute(ps.func, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(smem)));
+        allow_max_smem(ps.func, device);
     }
     return ps;
 }
