@@ -70,27 +70,36 @@ def newer(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def generate_specializations():
+    sys.path.insert(0, CSRC)
+    import gen_specializations
+
+    return gen_specializations.main(os.path.join(BUILD, 'gen'))
+
+
 def build(verbose=False, jobs=None):
     os.makedirs(OUTDIR, exist_ok=True)
     os.makedirs(BUILD, exist_ok=True)
     cuda = cuda_home()
     nvcc = os.path.join(cuda, 'bin', 'nvcc')
     embed_engine()
+    gen_units = generate_specializations()
     headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC)
                if h.endswith(('.h', '.hpp', '.cuh'))] + [os.path.join(INCLUDE, 'bbfft_gb300.h')]
     common_inc = ['-I' + CSRC, '-I' + INCLUDE, '-I' + BUILD, '-I' + os.path.join(cuda, 'include')]
     jobs_list = []
     objs = []
-    for u in KERNEL_UNITS:
-        src = os.path.join(CSRC, u)
+    for src in [os.path.join(CSRC, u) for u in KERNEL_UNITS] + gen_units:
+        u = os.path.basename(src)
         obj = os.path.join(BUILD, u + '.o')
         objs.append(obj)
         if newer(obj, [src] + headers):
             jobs_list.append([nvcc, ARCH, '-lineinfo', '-O3', '-std=c++17', '-Xcompiler', '-fPIC',
-                              '-Xptxas', '-v', '-c', src, '-o', obj] + common_inc)
+                              '-Xcompiler', '-fvisibility=hidden', '-Xptxas', '-v', '-c', src,
+                              '-o', obj] + common_inc)
     cxx = os.environ.get('CXX', 'g++')
-    for u in HOST_UNITS:
-        src = os.path.join(CSRC, u)
+    for src in [os.path.join(CSRC, u) for u in HOST_UNITS] + [os.path.join(BUILD, 'gen', 'ct_index.cpp')]:
+        u = os.path.basename(src)
         obj = os.path.join(BUILD, u + '.o')
         objs.append(obj)
         if newer(obj, [src] + headers + [os.path.join(BUILD, 'engine_src.inc')]):

@@ -1,0 +1,165 @@
+#!/usr/bin/env python3
+"""Generate the compile-time-size kernel instantiations and their look-up table.
+
+For every complex FFT length Nc in the lists below and every transform kind that uses
+it, one kernel fft_kernel_ct<R, Kind, Nc, T, radices...> is instantiated with the radices
+and threads-per-transform that the host heuristic (choose_radices in library.cpp,
+restated here as choose_radices) picks.  The host looks a plan up in the generated
+table and falls back to the runtime-size kernel when there is no entry.
+
+Usage: gen_specializations.py OUTDIR   (writes kernels_ct_<prec>_<kind>.cu, ct_index.cpp)
+"""
+import os
+import sys
+
+# complex FFT lengths with compile-time kernels
+EVEN_NC = [2, 4, 8, 16, 32, 64, 128, 256, 512, 24, 48, 80, 96, 112, 160, 192, 224, 384]
+ODD_NC = [3, 5, 7, 9, 11, 13, 15, 25, 27]
+KINDS = {0: 'c2c', 1: 'r2ch', 2: 'r2cf', 3: 'c2rh', 4: 'c2rf'}
+UNROLLED = set(range(1, 14)) | {16}
+
+
+def prime_factors(n):
+    f, p = [], 2
+    while n > 1:
+        if n % p == 0:
+            f.append(p)
+            n //= p
+        else:
+            p += 1
+    return f
+
+
+def choose_radices(nc):
+    """Same rule as choose_radices() in library.cpp."""
+    if nc == 1:
+        return [1]
+    c2 = c3 = 0
+    odd, big = [], []
+    for p in prime_factors(nc):
+        if p == 2:
+            c2 += 1
+        elif p == 3:
+            c3 += 1
+        elif p <= 13:
+            odd.append(p)
+        else:
+            big.append(p)
+    r = []
+    while c3 >= 2:
+        r.append(9)
+        c3 -= 2
+    if c3 == 1:
+        if c2 >= 2 and c2 != 3 and c2 != 6:
+            r.append(12)
+            c2 -= 2
+        elif c2 >= 1:
+            r.append(6)
+            c2 -= 1
+        else:
+            r.append(3)
+    for p in odd:
+        if p == 5 and c2 >= 1 and c2 % 3 == 1:
+            r.append(10)
+            c2 -= 1
+        else:
+            r.append(p)
+    if c2 > 0:
+        chunks = (c2 + 3) // 4
+        for i in range(chunks):
+            bits = c2 // chunks + (1 if i < c2 % chunks else 0)
+            r.append(1 << bits)
+    r.sort(reverse=True)
+    return r + big
+
+
+def stage_list(nc, kind):
+    """Radices incl. the copy stages the host adds, and threads per transform."""
+    rad = choose_radices(nc)
+    if rad[0] not in UNROLLED:
+        rad = [1] + rad
+    real = kind != 0
+    post = kind == 1
+    if real and not post and len(rad) == 1:
+        rad = rad + [1]
+    pu = max([r for r in rad if r in UNROLLED] + [1])
+    T = max(1, nc // pu) if pu > 1 else min(nc, 64)
+    T = min(T, 512)
+    return rad, T
+
+
+def entries():
+    out = []
+    for prec in (4, 8):
+        for kind in KINDS:
+            ncs = EVEN_NC + ODD_NC if kind == 0 else (EVEN_NC if kind in (1, 3) else ODD_NC)
+            for nc in ncs:
+                rad, T = stage_list(nc, kind)
+                if any(r not in UNROLLED for r in rad):
+                    continue
+                out.append((prec, kind, nc, T, rad))
+    return out
+
+
+def main(outdir):
+    os.makedirs(outdir, exist_ok=True)
+    ents = entries()
+    files = {}
+    for prec, kind, nc, T, rad in ents:
+        files.setdefault((prec, kind), []).append((nc, T, rad))
+    index = ['// generated by gen_specializations.py', '#include "kernels.hpp"', '',
+             'namespace gbfft {']
+    tables = []
+    for (prec, kind), lst in sorted(files.items()):
+        R = 'float' if prec == 4 else 'double'
+        name = 'ct_table_f%d_%s' % (prec * 8, KINDS[kind])
+        src = ['// generated by gen_specializations.py: compile-time-size FFT kernels',
+               '#include "engine.cuh"', '#include "kernels.hpp"', '', 'namespace gbfft {', '',
+               'template <class R, int Kind, int NC, int TT, int... Ps>',
+               '__global__ void __launch_bounds__(512) fft_kernel_ct(const __grid_constant__ fft_params p) {',
+               '    fft_tile_ct<R, Kind, default_io, NC, TT, Ps...>(p);', '}', '',
+               'extern const ct_entry %s[] = {' % name]
+        for nc, T, rad in lst:
+            rs = ', '.join(map(str, rad))
+            src.append('    {%d, %d, %d, %d, %d, {%s}, reinterpret_cast<const void *>(&fft_kernel_ct<%s, %d, %d, %d, %s>)},'
+                       % (prec, kind, nc, T, len(rad), rs, R, kind, nc, T, rs))
+        src += ['};', 'extern const int %s_size = %d;' % (name, len(lst)), '', '} // namespace gbfft', '']
+        fn = os.path.join(outdir, 'kernels_ct_f%d_%s.cu' % (prec * 8, KINDS[kind]))
+        text = '\n'.join(src)
+        if not os.path.exists(fn) or open(fn).read() != text:
+            with open(fn, 'w') as f:
+                f.write(text)
+        index.append('extern const ct_entry %s[];' % name)
+        index.append('extern const int %s_size;' % name)
+        tables.append(name)
+    index += ['', 'static const ct_entry *const kTables[] = {%s};' % ', '.join(tables),
+              'static const int *const kSizes[] = {%s};' % ', '.join('&%s_size' % t for t in tables),
+              '',
+              'const ct_entry *ct_lookup(int prec, int kind, int nc, int T, const int *rad, int L) {',
+              '    for (unsigned t = 0; t < sizeof(kTables) / sizeof(kTables[0]); ++t) {',
+              '        for (int i = 0; i < *kSizes[t]; ++i) {',
+              '            const ct_entry &e = kTables[t][i];',
+              '            if (e.prec != prec || e.kind != kind || e.nc != nc || e.T != T || e.L != L) {',
+              '                continue;',
+              '            }',
+              '            bool same = true;',
+              '            for (int s = 0; s < L; ++s) {',
+              '                same = same && e.rad[s] == rad[s];',
+              '            }',
+              '            if (same) {',
+              '                return &e;',
+              '            }',
+              '        }',
+              '    }',
+              '    return nullptr;',
+              '}', '', '} // namespace gbfft', '']
+    fn = os.path.join(outdir, 'ct_index.cpp')
+    text = '\n'.join(index)
+    if not os.path.exists(fn) or open(fn).read() != text:
+        with open(fn, 'w') as f:
+            f.write(text)
+    return sorted(os.path.join(outdir, 'kernels_ct_f%d_%s.cu' % (p * 8, KINDS[k])) for p, k in files)
+
+
+if __name__ == '__main__':
+    print('\n'.join(main(sys.argv[1])))

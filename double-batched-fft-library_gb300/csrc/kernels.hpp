@@ -2,6 +2,21 @@
 #pragma once
 
 namespace gbfft {
+
+// runtime-size kernels, one per transform kind
 const void *kernel_f32(int kind);
 const void *kernel_f64(int kind);
+
+// compile-time-size kernels (generated by gen_specializations.py)
+struct ct_entry {
+    int prec;    // bytes per real
+    int kind;    // gbfft::kind
+    int nc;      // complex FFT length
+    int T;       // threads per transform
+    int L;       // number of stages
+    int rad[12]; // radices
+    const void *fn;
+};
+const ct_entry *ct_lookup(int prec, int kind, int nc, int T, const int *rad, int L);
+
 } // namespace gbfft

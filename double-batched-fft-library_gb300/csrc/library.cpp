@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -341,6 +342,7 @@ struct pass {
     std::shared_ptr<module> mod;
     std::shared_ptr<device_buffer> tw;
     bool inplace_ok = true;
+    bool specialized = false; // compile-time-size kernel
     std::string identifier;
     int in_sel = 0;  // 0: user input, 2: temporary
     int out_sel = 1; // 1: user output, 2: temporary
@@ -415,6 +417,109 @@ static char const *kind_name(int kind) {
     return "?";
 }
 
+// Shared-memory bank model: wavefronts needed by one warp request of 8-byte (complex
+// float) or 16-byte (complex double) elements; each wavefront serves 128 bytes and a bank
+// conflict occurs when two lanes of a wavefront touch different words of one bank.
+static int wavefronts(int const *elem, int lanes, int elem_bytes) {
+    int per = 128 / elem_bytes; // lanes served per wavefront without conflicts
+    int words = elem_bytes / 4;
+    int total = 0;
+    for (int g = 0; g < lanes; g += per) {
+        int worst = 1;
+        for (int bank = 0; bank < 32; ++bank) {
+            int distinct[32];
+            int nd = 0;
+            for (int l = g; l < g + per && l < lanes; ++l) {
+                if (elem[l] < 0) {
+                    continue;
+                }
+                for (int w = 0; w < words; ++w) {
+                    int word = elem[l] * words + w;
+                    if (word % 32 != bank) {
+                        continue;
+                    }
+                    bool seen = false;
+                    for (int d = 0; d < nd; ++d) {
+                        seen = seen || distinct[d] == word;
+                    }
+                    if (!seen && nd < 32) {
+                        distinct[nd++] = word;
+                    }
+                }
+            }
+            worst = std::max(worst, nd);
+        }
+        total += worst;
+    }
+    return total;
+}
+
+// Pick the shared-memory padding that minimises the modelled wavefronts of the first warp
+// over all shared accesses of the stages (Stockham reads/writes and the r2c post-process).
+void choose_padding(fft_params &p, int prec, bool post) {
+    static const int cands[][2] = {{4, 1}, {3, 1}, {5, 1}, {6, 8}, {5, 8}, {7, 8},
+                                   {4, 2}, {5, 2}, {6, 4}, {30, 0}};
+    int const eb = 2 * prec;
+    int const lanes = 32;
+    int best = -1, best_cost = 1 << 30;
+    for (int ci = 0; ci < static_cast<int>(sizeof(cands) / sizeof(cands[0])); ++ci) {
+        int sh = cands[ci][0], ad = cands[ci][1];
+        auto idx = [&](int k_l, int n, int m_l) {
+            int i = (k_l * p.Nc + n) * p.Mb + m_l;
+            return i + (i >> sh) * ad;
+        };
+        long cost = 0;
+        int Ns = 1;
+        for (int s = 0; s < p.L; ++s) {
+            int P = p.radix[s];
+            bool src_g = s == 0;
+            bool dst_g = s == p.L - 1 && !post;
+            int nb = p.Nc / P;
+            for (int r = 0; r < P && r < 16; ++r) {
+                int rd[32], wr[32];
+                for (int l = 0; l < lanes; ++l) {
+                    int m_l = l % p.Mb, j = (l / p.Mb) % p.T, k_l = l / (p.Mb * p.T);
+                    rd[l] = wr[l] = -1;
+                    if (k_l >= p.Kb || j >= nb) {
+                        continue;
+                    }
+                    int b = j;
+                    int o = b + (b / Ns) * Ns * (P - 1);
+                    rd[l] = idx(k_l, b + r * nb, m_l);
+                    wr[l] = idx(k_l, o + r * Ns, m_l);
+                }
+                if (!src_g) {
+                    cost += wavefronts(rd, lanes, eb);
+                }
+                if (!dst_g) {
+                    cost += wavefronts(wr, lanes, eb);
+                }
+            }
+            Ns *= P;
+        }
+        if (post) {
+            int a[32], b2[32];
+            for (int l = 0; l < lanes; ++l) {
+                int m_l = l % p.Mb, j = (l / p.Mb) % p.T, k_l = l / (p.Mb * p.T);
+                a[l] = b2[l] = -1;
+                if (k_l >= p.Kb || 2 * j > p.Nc) {
+                    continue;
+                }
+                a[l] = idx(k_l, j, m_l);
+                b2[l] = idx(k_l, (p.Nc - j) % p.Nc, m_l);
+            }
+            cost += wavefronts(a, lanes, eb) + wavefronts(b2, lanes, eb);
+        }
+        // prefer less padding on ties (cands are ordered by preference)
+        if (cost < best_cost) {
+            best_cost = static_cast<int>(cost);
+            best = ci;
+        }
+    }
+    p.pad_shift = cands[best][0];
+    p.pad_add = cands[best][1];
+}
+
 pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     pass ps;
     ps.prec = q.prec;
@@ -464,15 +569,14 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
             bad_config("product of radices must equal the complex FFT length " + std::to_string(Nc));
         }
     }
-    bool pre = ps.kind == kind_c2r_half;
     bool post = ps.kind == kind_r2c_half;
     // a generic (non-unrolled) first stage needs a shared-memory source
-    if (!pre && !unrolled(rad.front())) {
+    if (!unrolled(rad.front())) {
         rad.insert(rad.begin(), 1);
     }
     // real transforms must finish all global reads of a tile before the first global write
     // (in-place safety): with a single global->global stage, add a shared round trip
-    if (is_real && !pre && !post && rad.size() == 1) {
+    if (is_real && !post && rad.size() == 1) {
         rad.push_back(1);
     }
     if (rad.size() > static_cast<std::size_t>(max_stages)) {
@@ -481,7 +585,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     int L = static_cast<int>(rad.size());
     int nbuf = 1;
     for (int s = 0; s < L; ++s) {
-        bool src_g = s == 0 && !pre;
+        bool src_g = s == 0;
         bool dst_g = s == L - 1 && !post;
         if (!src_g && !dst_g) {
             nbuf = 2;
@@ -514,11 +618,10 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         Mb = (Mb + 1) / 2;
     }
     std::size_t celem = 2 * static_cast<std::size_t>(q.prec);
+    // shared padding i -> i + (i >> shift) * add adds at most a quarter (choose_padding)
     auto buf_elems = [&](int kb) {
-        long long n = static_cast<long long>(kb) * Nc * Mb;
-        long long last = n - 1;
-        long long padded = q.prec == 4 ? last + (last >> 4) : last + (last >> 3);
-        return padded + 1;
+        long long last = static_cast<long long>(kb) * Nc * Mb - 1;
+        return last + (last >> 2) + 1;
     };
     int Kb = q.Kb > 0 ? q.Kb : std::max(1, 256 / (Mb * T));
     Kb = static_cast<int>(std::min<long long>(Kb, K));
@@ -544,9 +647,12 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     fft_params &p = ps.p;
     p.M = M;
     p.K = K;
-    p.is1 = q.is1;
+    if ((N + 1) * std::max(std::llabs(q.is1), std::llabs(q.os1)) > 0x7fffffffLL) {
+        bad_config("stride of the FFT mode too large");
+    }
+    p.is1 = static_cast<int>(q.is1);
     p.is2 = q.is2;
-    p.os1 = q.os1;
+    p.os1 = static_cast<int>(q.os1);
     p.os2 = q.os2;
     p.N = N;
     p.Nc = Nc;
@@ -561,8 +667,20 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     p.m_tiles = static_cast<int>((M + Mb - 1) / Mb);
     p.flags = flags;
     p.nbuf = nbuf;
-    p.buf_elems = static_cast<int>(buf_elems(Kb));
     p.scale = 1.0;
+    choose_padding(p, q.prec, post);
+    {
+        long long last = static_cast<long long>(Kb) * Nc * Mb - 1;
+        p.buf_elems = static_cast<int>(last + (last >> p.pad_shift) * p.pad_add + 1);
+    }
+    smem = static_cast<std::size_t>(nbuf) * p.buf_elems * celem;
+    // paired real loads / stores: adjacent (unit N-stride, one transform per M) and aligned
+    if (ps.kind == kind_r2c_half && q.is1 == 1 && M == 1 && q.is2 % 2 == 0) {
+        p.flags |= flag_vec_in;
+    }
+    if (ps.kind == kind_c2r_half && q.os1 == 1 && M == 1 && q.os2 % 2 == 0) {
+        p.flags |= flag_vec_out;
+    }
     long long k_tiles = (K + Kb - 1) / Kb;
     if (static_cast<long long>(p.m_tiles) * k_tiles > 0x7fffffffLL) {
         bad_config("tensor too large for one launch");
@@ -592,7 +710,9 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     ps.identifier = c_ident(id.str());
 
     if (!has_cb) {
-        ps.func = q.prec == 4 ? kernel_f32(ps.kind) : kernel_f64(ps.kind);
+        const ct_entry *ct = ct_lookup(q.prec, ps.kind, Nc, T, rad.data(), L);
+        ps.func = ct ? ct->fn : (q.prec == 4 ? kernel_f32(ps.kind) : kernel_f64(ps.kind));
+        ps.specialized = ct != nullptr;
         if (!ps.func) {
             throw status_error(BBFFT_INTERNAL_ERROR, "kernel not found");
         }
@@ -858,6 +978,14 @@ static void execute_impl(bbfft_plan_s &plan, const void *in, void *out, cudaStre
         fft_params p = ps.p;
         p.in = ps.in_sel == 0 ? in : tmp;
         p.out = ps.out_sel == 1 ? out : tmp;
+        // paired real accesses need pointers aligned to one complex element
+        std::uintptr_t const align = 2 * static_cast<std::uintptr_t>(ps.prec);
+        if (reinterpret_cast<std::uintptr_t>(p.in) % align) {
+            p.flags &= ~flag_vec_in;
+        }
+        if (reinterpret_cast<std::uintptr_t>(p.out) % align) {
+            p.flags &= ~flag_vec_out;
+        }
         void *args[] = {&p};
         cudaError_t e = cudaLaunchKernel(ps.func, dim3(ps.grid), dim3(ps.block), args, ps.smem, stream);
         if (e != cudaSuccess) {

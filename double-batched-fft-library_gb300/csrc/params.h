@@ -8,20 +8,20 @@ constexpr int max_stages = 12;
 
 enum kind : int {
     kind_c2c = 0,
-    kind_r2c_half = 1, // even N
-    kind_r2c_full = 2, // odd N
-    kind_c2r_half = 3, // even N
-    kind_c2r_full = 4, // odd N
+    kind_r2c_half = 1, // even N: N/2-point complex FFT + post-process
+    kind_r2c_full = 2, // odd N: N-point complex FFT of real data
+    kind_c2r_half = 3, // even N: pre-process + N/2-point complex FFT
+    kind_c2r_full = 4, // odd N: N-point complex FFT of the Hermitian extension
 };
 
-
 // flags
-constexpr int flag_conj_in = 1;       // c2c: conjugate on load (backward)
-constexpr int flag_conj_out = 2;      // c2c: conjugate on store (backward)
-constexpr int flag_adj_r2c = 4;       // adjoint of r2c, run as a c2r kernel (Hermitian weights)
-constexpr int flag_adj_c2r = 8;       // adjoint of c2r, run as a r2c kernel (Hermitian weights)
-constexpr int flag_scale_out = 16;    // multiply the output by params.scale
-
+constexpr int flag_conj_in = 1;   // c2c: conjugate on load (backward)
+constexpr int flag_conj_out = 2;  // c2c: conjugate on store (backward)
+constexpr int flag_adj_r2c = 4;   // adjoint of r2c, run as a c2r kernel (Hermitian weights)
+constexpr int flag_adj_c2r = 8;   // adjoint of c2r, run as a r2c kernel (Hermitian weights)
+constexpr int flag_scale_out = 16; // multiply the output by params.scale
+constexpr int flag_vec_in = 32;   // real input pairs x[2n], x[2n+1] are adjacent and aligned
+constexpr int flag_vec_out = 64;  // real output pairs are adjacent and aligned
 
 struct fft_params {
     const void *in;
@@ -29,8 +29,8 @@ struct fft_params {
     const void *tw;        // w_Nt^{-i}, i = 0..Nt-1, complex of the plan precision
     long long M;           // left batch
     long long K;           // right batch
-    long long is1, is2;    // input strides of the N and K mode (elements)
-    long long os1, os2;    // output strides of the N and K mode (elements)
+    long long is2, os2;    // input / output strides of the K mode (elements)
+    int is1, os1;          // input / output strides of the N mode (elements)
     int N;                 // logical FFT length
     int Nc;                // complex FFT length (N or N/2)
     int Nt;                // twiddle table length
@@ -42,6 +42,7 @@ struct fft_params {
     int flags;
     int nbuf;              // shared buffers (1 or 2)
     int buf_elems;         // padded elements per buffer
+    int pad_shift, pad_add; // shared index i -> i + (i >> pad_shift) * pad_add
     double scale;          // used with flag_scale_out
 };
 
