@@ -437,34 +437,4 @@ template <class R, int Kind, class IO> __device__ __forceinline__ void fft_tile(
     }
 }
 
-// ---------------------------------------------------------- compile-time-size kernel body
-template <int L, bool Post> __host__ __device__ constexpr int ct_nbuf() { return (L >= 3 || (Post && L >= 2)) ? 2 : 1; }
-
-template <int NC, int TT, int NBUF, int S, int L, int NS, int CUR, class Ctx, int P, int... Rest>
-__device__ __forceinline__ void ct_stages(const Ctx &c, int j) {
-    constexpr bool post = Ctx::kind_v == kind_r2c_half;
-    constexpr bool src_g = S == 0;
-    constexpr bool dst_g = (S == L - 1) && !post;
-    constexpr int DST = (NBUF > 1 && !src_g) ? 1 - CUR : 0;
-    run_stage<P, NC, TT>(c, j, NS, src_g, CUR, dst_g, DST);
-    if constexpr (!dst_g) {
-        __syncthreads();
-    }
-    if constexpr (sizeof...(Rest) > 0) {
-        ct_stages<NC, TT, NBUF, S + 1, L, NS * P, DST, Ctx, Rest...>(c, j);
-    } else if constexpr (post) {
-        r2c_post<NC, TT>(c, j, DST);
-    }
-}
-
-template <class R, int Kind, class IO, int NC, int TT, int... Ps>
-__device__ __forceinline__ void fft_tile_ct(const fft_params &p) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    int j;
-    auto c = make_ctx<R, Kind, IO>(p, smem_raw, TT, NC, j);
-    constexpr int L = sizeof...(Ps);
-    constexpr bool post = Kind == kind_r2c_half;
-    ct_stages<NC, TT, ct_nbuf<L, post>(), 0, L, 1, 0, decltype(c), Ps...>(c, j);
-}
-
 } // namespace gbfft

@@ -1,0 +1,399 @@
+// Compile-time-size FFT kernels, vectorised over the left batch mode M.
+//
+// Same algorithm and data semantics as the runtime engine (engine.cuh), specialised for
+// a fixed complex length NC, radix list and threads per transform TT:
+//  * every index, trip count and twiddle stride is a compile-time constant;
+//  * each thread owns V consecutive m of the M-mode (M is the fastest-varying mode of the
+//    column-major tensor, so the V transforms sit next to each other in memory): global
+//    and shared accesses move V elements at once (16-byte vectors), and every twiddle load
+//    and index computation is shared by V transforms;
+//  * stages run in place in ONE shared buffer: a thread keeps all butterflies of a stage
+//    in registers, so after a barrier it can overwrite the values it read.
+#pragma once
+
+#include "engine.cuh"
+
+namespace gbfft {
+
+// ---- vector access of V consecutive elements (aligned to V * sizeof(element)) ----------
+template <int V> __device__ __forceinline__ void ldv(const float2 *p, float2 *o) {
+    if constexpr (V == 1) {
+        o[0] = p[0];
+    } else {
+        sfor<0, V / 2>([&](auto I) {
+            float4 q = reinterpret_cast<const float4 *>(p)[I.value];
+            o[2 * I.value] = mk<float>(q.x, q.y);
+            o[2 * I.value + 1] = mk<float>(q.z, q.w);
+        });
+    }
+}
+template <int V> __device__ __forceinline__ void stv(float2 *p, const float2 *o) {
+    if constexpr (V == 1) {
+        p[0] = o[0];
+    } else {
+        sfor<0, V / 2>([&](auto I) {
+            float4 q;
+            q.x = o[2 * I.value].x;
+            q.y = o[2 * I.value].y;
+            q.z = o[2 * I.value + 1].x;
+            q.w = o[2 * I.value + 1].y;
+            reinterpret_cast<float4 *>(p)[I.value] = q;
+        });
+    }
+}
+template <int V> __device__ __forceinline__ void ldv(const double2 *p, double2 *o) {
+    sfor<0, V>([&](auto I) { o[I.value] = p[I.value]; });
+}
+template <int V> __device__ __forceinline__ void stv(double2 *p, const double2 *o) {
+    sfor<0, V>([&](auto I) { p[I.value] = o[I.value]; });
+}
+template <int V> __device__ __forceinline__ void ldv(const float *p, float *o) {
+    if constexpr (V == 1) {
+        o[0] = p[0];
+    } else if constexpr (V == 2) {
+        float2 q = *reinterpret_cast<const float2 *>(p);
+        o[0] = q.x;
+        o[1] = q.y;
+    } else {
+        sfor<0, V / 4>([&](auto I) {
+            float4 q = reinterpret_cast<const float4 *>(p)[I.value];
+            o[4 * I.value] = q.x;
+            o[4 * I.value + 1] = q.y;
+            o[4 * I.value + 2] = q.z;
+            o[4 * I.value + 3] = q.w;
+        });
+    }
+}
+template <int V> __device__ __forceinline__ void stv(float *p, const float *o) {
+    if constexpr (V == 1) {
+        p[0] = o[0];
+    } else if constexpr (V == 2) {
+        *reinterpret_cast<float2 *>(p) = mk<float>(o[0], o[1]);
+    } else {
+        sfor<0, V / 4>([&](auto I) {
+            float4 q;
+            q.x = o[4 * I.value];
+            q.y = o[4 * I.value + 1];
+            q.z = o[4 * I.value + 2];
+            q.w = o[4 * I.value + 3];
+            reinterpret_cast<float4 *>(p)[I.value] = q;
+        });
+    }
+}
+template <int V> __device__ __forceinline__ void ldv(const double *p, double *o) {
+    if constexpr (V == 1) {
+        o[0] = p[0];
+    } else {
+        sfor<0, V / 2>([&](auto I) {
+            double2 q = reinterpret_cast<const double2 *>(p)[I.value];
+            o[2 * I.value] = q.x;
+            o[2 * I.value + 1] = q.y;
+        });
+    }
+}
+template <int V> __device__ __forceinline__ void stv(double *p, const double *o) {
+    if constexpr (V == 1) {
+        p[0] = o[0];
+    } else {
+        sfor<0, V / 2>([&](auto I) {
+            reinterpret_cast<double2 *>(p)[I.value] = mk<double>(o[2 * I.value], o[2 * I.value + 1]);
+        });
+    }
+}
+
+template <class R, int Kind, int NC, int TT, int V> struct ct_ctx {
+    using C = cplx<R>;
+    static constexpr int kind_v = Kind;
+    static constexpr bool half = Kind == kind_r2c_half || Kind == kind_c2r_half;
+    static constexpr int NN = half ? 2 * NC : NC; // logical length (odd kinds: N = NC)
+    const fft_params &p;
+    C *sm;
+    long long ib, ob;
+    int sbase; // shared index of element 0 of this thread's first transform
+    int pshift, padd;
+    bool active;
+
+    __device__ __forceinline__ int sidx(int n) const {
+        int i = sbase + n * p.Mb;
+        return i + (i >> pshift) * padd;
+    }
+
+    __device__ __forceinline__ C adj_r2c_weight(C v, int k) const {
+        if (k == 0 || 2 * k == NN) {
+            v.y = R(0);
+        } else {
+            v.x *= R(0.5);
+            v.y *= R(0.5);
+        }
+        return v;
+    }
+    __device__ __forceinline__ C adj_c2r_weight(C v, int k, R g0) const {
+        if (k == 0) {
+            v.y = R(0);
+        } else if (2 * k == NN) {
+            v.y = -g0;
+        } else {
+            v.x *= R(2);
+            v.y *= R(2);
+        }
+        return v;
+    }
+
+    __device__ __forceinline__ void gload(int n, C *o) const {
+        if constexpr (Kind == kind_c2c) {
+            ldv<V>(static_cast<const C *>(p.in) + ib + n * p.is1, o);
+            if (p.flags & flag_conj_in) {
+                sfor<0, V>([&](auto U) { o[U.value].y = -o[U.value].y; });
+            }
+        } else if constexpr (Kind == kind_r2c_half) {
+            const R *x = static_cast<const R *>(p.in) + ib;
+            if (V == 1 && (p.flags & flag_vec_in)) {
+                o[0] = reinterpret_cast<const C *>(x)[n];
+                return;
+            }
+            R a[V], b[V];
+            ldv<V>(x + (2 * n) * p.is1, a);
+            ldv<V>(x + (2 * n + 1) * p.is1, b);
+            sfor<0, V>([&](auto U) { o[U.value] = mk<R>(a[U.value], b[U.value]); });
+        } else if constexpr (Kind == kind_r2c_full) {
+            R a[V];
+            ldv<V>(static_cast<const R *>(p.in) + ib + n * p.is1, a);
+            sfor<0, V>([&](auto U) { o[U.value] = mk<R>(a[U.value], R(0)); });
+        } else if constexpr (Kind == kind_c2r_full) {
+            const C *X = static_cast<const C *>(p.in) + ib;
+            if (2 * n <= NN) {
+                ldv<V>(X + n * p.is1, o);
+                sfor<0, V>([&](auto U) {
+                    C v = o[U.value];
+                    if (n == 0) {
+                        v.y = R(0);
+                    }
+                    if (p.flags & flag_adj_r2c) {
+                        v = adj_r2c_weight(v, n);
+                    }
+                    v.y = -v.y;
+                    o[U.value] = v;
+                });
+            } else {
+                ldv<V>(X + (NN - n) * p.is1, o);
+                if (p.flags & flag_adj_r2c) {
+                    sfor<0, V>([&](auto U) { o[U.value] = adj_r2c_weight(o[U.value], NN - n); });
+                }
+            }
+        } else {
+            // c2r_half: Z[n] = (x1 + x2) + (x1 - x2) i w_N^{+n}, x1 = X[n], x2 = conj X[NC-n]
+            const C *X = static_cast<const C *>(p.in) + ib;
+            C x1[V], x2[V];
+            ldv<V>(X + n * p.is1, x1);
+            ldv<V>(X + (NC - n) * p.is1, x2);
+            C w = __ldg(static_cast<const C *>(p.tw) + n);
+            C iw = mk<R>(w.y, w.x);
+            sfor<0, V>([&](auto U) {
+                C a1 = x1[U.value], a2 = x2[U.value];
+                if (n == 0) {
+                    a1.y = R(0);
+                }
+                if (p.flags & flag_adj_r2c) {
+                    a1 = adj_r2c_weight(a1, n);
+                    a2 = adj_r2c_weight(a2, NC - n);
+                }
+                a2.y = -a2.y;
+                C a = cadd(a1, a2);
+                C b = cmul(csub(a1, a2), iw);
+                C z = cadd(a, b);
+                z.y = -z.y;
+                o[U.value] = z;
+            });
+        }
+    }
+
+    __device__ __forceinline__ void gstore(int n, C *v) const {
+        if constexpr (Kind == kind_c2c) {
+            if (p.flags & flag_conj_out) {
+                sfor<0, V>([&](auto U) { v[U.value].y = -v[U.value].y; });
+            }
+            if (p.flags & flag_scale_out) {
+                sfor<0, V>([&](auto U) {
+                    v[U.value].x *= R(p.scale);
+                    v[U.value].y *= R(p.scale);
+                });
+            }
+            stv<V>(static_cast<C *>(p.out) + ob + n * p.os1, v);
+        } else if constexpr (Kind == kind_r2c_full) {
+            if (2 * n <= NN) {
+                if (p.flags & flag_adj_c2r) {
+                    sfor<0, V>([&](auto U) { v[U.value] = adj_c2r_weight(v[U.value], n, R(0)); });
+                }
+                stv<V>(static_cast<C *>(p.out) + ob + n * p.os1, v);
+            }
+        } else if constexpr (Kind == kind_c2r_full) {
+            R a[V];
+            sfor<0, V>([&](auto U) { a[U.value] = v[U.value].x; });
+            stv<V>(static_cast<R *>(p.out) + ob + n * p.os1, a);
+        } else if constexpr (Kind == kind_c2r_half) {
+            R *x = static_cast<R *>(p.out) + ob;
+            if (V == 1 && (p.flags & flag_vec_out)) {
+                reinterpret_cast<C *>(x)[n] = mk<R>(v[0].x, -v[0].y);
+                return;
+            }
+            R a[V], b[V];
+            sfor<0, V>([&](auto U) {
+                a[U.value] = v[U.value].x;
+                b[U.value] = -v[U.value].y;
+            });
+            stv<V>(x + (2 * n) * p.os1, a);
+            stv<V>(x + (2 * n + 1) * p.os1, b);
+        }
+    }
+};
+
+// One in-place Stockham stage with compile-time sizes (see engine.cuh for the formulas).
+template <int P, int NS, bool SRC_G, bool DST_G, class Ctx, class R, int NC, int TT, int V>
+__device__ __forceinline__ void ct_stage(const Ctx &c, int j) {
+    using C = cplx<R>;
+    constexpr int nb = NC / P;
+    constexpr int ITERS = (nb + TT - 1) / TT;
+    constexpr int twstride = (Ctx::half ? 2 * NC : NC) / (NS * P);
+    const C *tw = static_cast<const C *>(c.p.tw);
+    C v[ITERS][V][P];
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int b = j + it * TT;
+        if (nb % TT == 0 || b < nb) {
+            if constexpr (SRC_G) {
+                if (c.active) {
+                    sfor<0, P>([&](auto I) {
+                        C t[V];
+                        c.gload(b + I.value * nb, t);
+                        sfor<0, V>([&](auto U) { v[it][U.value][I.value] = t[U.value]; });
+                    });
+                } else {
+                    sfor<0, P>([&](auto I) {
+                        sfor<0, V>([&](auto U) { v[it][U.value][I.value] = mk<R>(R(0), R(0)); });
+                    });
+                }
+            } else {
+                sfor<0, P>([&](auto I) {
+                    C t[V];
+                    ldv<V>(c.sm + c.sidx(b + I.value * nb), t);
+                    sfor<0, V>([&](auto U) { v[it][U.value][I.value] = t[U.value]; });
+                });
+            }
+            if constexpr (P > 1 && NS > 1) {
+                const int kk = b % NS;
+                sfor<1, P>([&](auto I) {
+                    C w = __ldg(tw + I.value * kk * twstride);
+                    sfor<0, V>([&](auto U) { v[it][U.value][I.value] = cmul(v[it][U.value][I.value], w); });
+                });
+            }
+            sfor<0, V>([&](auto U) { dft<P, R>::run(v[it][U.value]); });
+        }
+    }
+    if constexpr (!SRC_G && !DST_G) {
+        __syncthreads(); // every value of the buffer is read before it is overwritten
+    }
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int b = j + it * TT;
+        if (nb % TT == 0 || b < nb) {
+            const int o = b + (b / NS) * NS * (P - 1);
+            sfor<0, P>([&](auto I) {
+                C t[V];
+                sfor<0, V>([&](auto U) { t[U.value] = v[it][U.value][I.value]; });
+                if constexpr (DST_G) {
+                    if (c.active) {
+                        c.gstore(o + I.value * NS, t);
+                    }
+                } else {
+                    stv<V>(c.sm + c.sidx(o + I.value * NS), t);
+                }
+            });
+        }
+    }
+}
+
+// r2c (even N) post-process from the shared buffer, V transforms per thread.
+template <class Ctx, class R, int NC, int TT, int V>
+__device__ __forceinline__ void ct_r2c_post(const Ctx &c, int j) {
+    using C = cplx<R>;
+    const C *tw = static_cast<const C *>(c.p.tw);
+    constexpr int cnt = NC / 2 + 1;
+    constexpr int ITERS = (cnt + TT - 1) / TT;
+    R g0[V];
+    if (c.p.flags & flag_adj_c2r) {
+        C z0[V];
+        ldv<V>(c.sm + c.sidx(0), z0);
+        sfor<0, V>([&](auto U) { g0[U.value] = z0[U.value].x + z0[U.value].y; });
+    }
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int i = j + it * TT;
+        if (cnt % TT == 0 || i < cnt) {
+            const int io = NC - i;
+            C y1[V], y2[V], xi[V], xo[V];
+            ldv<V>(c.sm + c.sidx(i), y1);
+            ldv<V>(c.sm + c.sidx(io == NC ? 0 : io), y2);
+            C w = __ldg(tw + i);
+            C iw = mk<R>(-w.y, w.x);
+            sfor<0, V>([&](auto U) {
+                C a2 = y2[U.value], a1 = y1[U.value];
+                a2.y = -a2.y;
+                C a = mk<R>((a2.x + a1.x) * R(0.5), (a2.y + a1.y) * R(0.5));
+                C b = mk<R>((a2.x - a1.x) * R(0.5), (a2.y - a1.y) * R(0.5));
+                b = cmul(b, iw);
+                C p1 = cadd(a, b);
+                C p2 = mk<R>(a.x - b.x, b.y - a.y);
+                if (c.p.flags & flag_adj_c2r) {
+                    p1 = c.adj_c2r_weight(p1, i, g0[U.value]);
+                    p2 = c.adj_c2r_weight(p2, io, g0[U.value]);
+                }
+                xi[U.value] = p1;
+                xo[U.value] = p2;
+            });
+            if (c.active) {
+                C *X = static_cast<C *>(c.p.out) + c.ob;
+                stv<V>(X + i * c.p.os1, xi);
+                if (i != io) {
+                    stv<V>(X + io * c.p.os1, xo);
+                }
+            }
+        }
+    }
+}
+
+template <class Ctx, class R, int NC, int TT, int V, int S, int L, int NS, int P, int... Rest>
+__device__ __forceinline__ void ct_run(const Ctx &c, int j) {
+    constexpr bool post = Ctx::kind_v == kind_r2c_half;
+    constexpr bool src_g = S == 0;
+    constexpr bool dst_g = (S == L - 1) && !post;
+    ct_stage<P, NS, src_g, dst_g, Ctx, R, NC, TT, V>(c, j);
+    if constexpr (!dst_g) {
+        __syncthreads();
+    }
+    if constexpr (sizeof...(Rest) > 0) {
+        ct_run<Ctx, R, NC, TT, V, S + 1, L, NS * P, Rest...>(c, j);
+    } else if constexpr (post) {
+        ct_r2c_post<Ctx, R, NC, TT, V>(c, j);
+    }
+}
+
+template <class R, int Kind, int NC, int TT, int V, int... Ps>
+__device__ __forceinline__ void fft_tile_ct(const fft_params &p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    using Ctx = ct_ctx<R, Kind, NC, TT, V>;
+    const int tid = threadIdx.x;
+    const int mvb = p.Mb / V;
+    const int mv = tid % mvb;
+    const int j = (tid / mvb) % TT;
+    const int k_l = tid / (mvb * TT);
+    const long long mt = blockIdx.x % p.m_tiles;
+    const long long kt = blockIdx.x / p.m_tiles;
+    const int m_l = mv * V;
+    const long long m = mt * p.Mb + m_l;
+    const long long k = kt * p.Kb + k_l;
+    Ctx c{p, reinterpret_cast<cplx<R> *>(smem_raw), m + k * p.is2, m + k * p.os2,
+          k_l * NC * p.Mb + m_l, p.pad_shift, p.pad_add, (m < p.M) && (k < p.K)};
+    ct_run<Ctx, R, NC, TT, V, 0, sizeof...(Ps), 1, Ps...>(c, j);
+}
+
+} // namespace gbfft

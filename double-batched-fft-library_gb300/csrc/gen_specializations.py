@@ -88,6 +88,18 @@ def stage_list(nc, kind):
     return rad, T
 
 
+def vector_width(prec, rad):
+    """Transforms per thread along M (same rule as vector_width() in library.cpp): keep
+    V * max radix complex values within 32 (float) / 16 (double) registers pairs."""
+    pmax = max(rad)
+    vmax = 4 if prec == 4 else 2
+    budget = 32 if prec == 4 else 16
+    v = vmax
+    while v > 1 and v * pmax > budget:
+        v //= 2
+    return v
+
+
 def entries():
     out = []
     for prec in (4, 8):
@@ -97,7 +109,8 @@ def entries():
                 rad, T = stage_list(nc, kind)
                 if any(r not in UNROLLED for r in rad):
                     continue
-                out.append((prec, kind, nc, T, rad))
+                for V in sorted({1, vector_width(prec, rad)}):
+                    out.append((prec, kind, nc, T, rad, V))
     return out
 
 
@@ -105,8 +118,8 @@ def main(outdir):
     os.makedirs(outdir, exist_ok=True)
     ents = entries()
     files = {}
-    for prec, kind, nc, T, rad in ents:
-        files.setdefault((prec, kind), []).append((nc, T, rad))
+    for prec, kind, nc, T, rad, V in ents:
+        files.setdefault((prec, kind), []).append((nc, T, rad, V))
     index = ['// generated by gen_specializations.py', '#include "kernels.hpp"', '',
              'namespace gbfft {']
     tables = []
@@ -114,15 +127,15 @@ def main(outdir):
         R = 'float' if prec == 4 else 'double'
         name = 'ct_table_f%d_%s' % (prec * 8, KINDS[kind])
         src = ['// generated by gen_specializations.py: compile-time-size FFT kernels',
-               '#include "engine.cuh"', '#include "kernels.hpp"', '', 'namespace gbfft {', '',
-               'template <class R, int Kind, int NC, int TT, int... Ps>',
-               '__global__ void __launch_bounds__(512) fft_kernel_ct(const __grid_constant__ fft_params p) {',
-               '    fft_tile_ct<R, Kind, default_io, NC, TT, Ps...>(p);', '}', '',
+               '#include "engine_ct.cuh"', '#include "kernels.hpp"', '', 'namespace gbfft {', '',
+               'template <class R, int Kind, int NC, int TT, int V, int... Ps>',
+               '__global__ void __launch_bounds__(256, 2) fft_kernel_ct(const __grid_constant__ fft_params p) {',
+               '    fft_tile_ct<R, Kind, NC, TT, V, Ps...>(p);', '}', '',
                'extern const ct_entry %s[] = {' % name]
-        for nc, T, rad in lst:
+        for nc, T, rad, V in lst:
             rs = ', '.join(map(str, rad))
-            src.append('    {%d, %d, %d, %d, %d, {%s}, reinterpret_cast<const void *>(&fft_kernel_ct<%s, %d, %d, %d, %s>)},'
-                       % (prec, kind, nc, T, len(rad), rs, R, kind, nc, T, rs))
+            src.append('    {%d, %d, %d, %d, %d, %d, {%s}, reinterpret_cast<const void *>(&fft_kernel_ct<%s, %d, %d, %d, %d, %s>)},'
+                       % (prec, kind, nc, T, V, len(rad), rs, R, kind, nc, T, V, rs))
         src += ['};', 'extern const int %s_size = %d;' % (name, len(lst)), '', '} // namespace gbfft', '']
         fn = os.path.join(outdir, 'kernels_ct_f%d_%s.cu' % (prec * 8, KINDS[kind]))
         text = '\n'.join(src)
@@ -135,11 +148,11 @@ def main(outdir):
     index += ['', 'static const ct_entry *const kTables[] = {%s};' % ', '.join(tables),
               'static const int *const kSizes[] = {%s};' % ', '.join('&%s_size' % t for t in tables),
               '',
-              'const ct_entry *ct_lookup(int prec, int kind, int nc, int T, const int *rad, int L) {',
+              'const ct_entry *ct_lookup(int prec, int kind, int nc, int T, int V, const int *rad, int L) {',
               '    for (unsigned t = 0; t < sizeof(kTables) / sizeof(kTables[0]); ++t) {',
               '        for (int i = 0; i < *kSizes[t]; ++i) {',
               '            const ct_entry &e = kTables[t][i];',
-              '            if (e.prec != prec || e.kind != kind || e.nc != nc || e.T != T || e.L != L) {',
+              '            if (e.prec != prec || e.kind != kind || e.nc != nc || e.T != T || e.V != V || e.L != L) {',
               '                continue;',
               '            }',
               '            bool same = true;',

@@ -13,10 +13,11 @@ struct ct_entry {
     int kind;    // gbfft::kind
     int nc;      // complex FFT length
     int T;       // threads per transform
+    int V;       // transforms per thread along M
     int L;       // number of stages
     int rad[12]; // radices
     const void *fn;
 };
-const ct_entry *ct_lookup(int prec, int kind, int nc, int T, const int *rad, int L);
+const ct_entry *ct_lookup(int prec, int kind, int nc, int T, int V, const int *rad, int L);
 
 } // namespace gbfft

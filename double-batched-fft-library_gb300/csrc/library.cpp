@@ -343,6 +343,8 @@ struct pass {
     std::shared_ptr<device_buffer> tw;
     bool inplace_ok = true;
     bool specialized = false; // compile-time-size kernel
+    int V = 1;                // transforms per thread along M
+    std::shared_ptr<pass> scalar_alt; // V = 1 variant for pointers not aligned to 16 bytes
     std::string identifier;
     int in_sel = 0;  // 0: user input, 2: temporary
     int out_sel = 1; // 1: user output, 2: temporary
@@ -360,6 +362,7 @@ struct pass_request {
     // tuning overrides
     std::vector<int> radices;
     int T = 0, Mb = 0, Kb = 0;
+    bool force_v1 = false;
 };
 
 static int max_optin_smem(int device) {
@@ -417,11 +420,24 @@ static char const *kind_name(int kind) {
     return "?";
 }
 
+// Transforms per thread along M for the compile-time kernels: V * max radix complex
+// values stay within 32 (float) / 16 (double) register pairs (gen_specializations.py
+// instantiates the same widths).
+static int vector_width(int prec, std::vector<int> const &rad) {
+    int pmax = *std::max_element(rad.begin(), rad.end());
+    int v = prec == 4 ? 4 : 2;
+    int budget = prec == 4 ? 32 : 16;
+    while (v > 1 && v * pmax > budget) {
+        v /= 2;
+    }
+    return v;
+}
+
 // Shared-memory bank model: wavefronts needed by one warp request of 8-byte (complex
 // float) or 16-byte (complex double) elements; each wavefront serves 128 bytes and a bank
 // conflict occurs when two lanes of a wavefront touch different words of one bank.
 static int wavefronts(int const *elem, int lanes, int elem_bytes) {
-    int per = 128 / elem_bytes; // lanes served per wavefront without conflicts
+    int per = std::max(1, 128 / elem_bytes); // lanes served per wavefront without conflicts
     int words = elem_bytes / 4;
     int total = 0;
     for (int g = 0; g < lanes; g += per) {
@@ -456,20 +472,27 @@ static int wavefronts(int const *elem, int lanes, int elem_bytes) {
 
 // Pick the shared-memory padding that minimises the modelled wavefronts of the first warp
 // over all shared accesses of the stages (Stockham reads/writes and the r2c post-process).
-void choose_padding(fft_params &p, int prec, bool post) {
+void choose_padding(fft_params &p, int prec, bool post, int V, bool inplace_stages) {
     static const int cands[][2] = {{4, 1}, {3, 1}, {5, 1}, {6, 8}, {5, 8}, {7, 8},
                                    {4, 2}, {5, 2}, {6, 4}, {30, 0}};
-    int const eb = 2 * prec;
+    // a lane moves V consecutive elements: the access is modelled as one element of V
+    // times the size; vectors must stay contiguous and 16-byte aligned after padding
+    int const eb = 2 * prec * V;
     int const lanes = 32;
+    int const mvb = p.Mb / V;
     int best = -1, best_cost = 1 << 30;
     for (int ci = 0; ci < static_cast<int>(sizeof(cands) / sizeof(cands[0])); ++ci) {
         int sh = cands[ci][0], ad = cands[ci][1];
+        if (V > 1 && ((1 << sh) < V || (prec == 4 && ad % 2 != 0))) {
+            continue;
+        }
         auto idx = [&](int k_l, int n, int m_l) {
             int i = (k_l * p.Nc + n) * p.Mb + m_l;
-            return i + (i >> sh) * ad;
+            return (i + (i >> sh) * ad) / V; // in units of the lane's vector
         };
         long cost = 0;
         int Ns = 1;
+        (void)inplace_stages;
         for (int s = 0; s < p.L; ++s) {
             int P = p.radix[s];
             bool src_g = s == 0;
@@ -478,7 +501,7 @@ void choose_padding(fft_params &p, int prec, bool post) {
             for (int r = 0; r < P && r < 16; ++r) {
                 int rd[32], wr[32];
                 for (int l = 0; l < lanes; ++l) {
-                    int m_l = l % p.Mb, j = (l / p.Mb) % p.T, k_l = l / (p.Mb * p.T);
+                    int m_l = (l % mvb) * V, j = (l / mvb) % p.T, k_l = l / (mvb * p.T);
                     rd[l] = wr[l] = -1;
                     if (k_l >= p.Kb || j >= nb) {
                         continue;
@@ -500,7 +523,7 @@ void choose_padding(fft_params &p, int prec, bool post) {
         if (post) {
             int a[32], b2[32];
             for (int l = 0; l < lanes; ++l) {
-                int m_l = l % p.Mb, j = (l / p.Mb) % p.T, k_l = l / (p.Mb * p.T);
+                int m_l = (l % mvb) * V, j = (l / mvb) % p.T, k_l = l / (mvb * p.T);
                 a[l] = b2[l] = -1;
                 if (k_l >= p.Kb || 2 * j > p.Nc) {
                     continue;
@@ -583,14 +606,6 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         bad_config("too many stages");
     }
     int L = static_cast<int>(rad.size());
-    int nbuf = 1;
-    for (int s = 0; s < L; ++s) {
-        bool src_g = s == 0;
-        bool dst_g = s == L - 1 && !post;
-        if (!src_g && !dst_g) {
-            nbuf = 2;
-        }
-    }
     int pu = 1;
     for (int r : rad) {
         if (unrolled(r)) {
@@ -604,41 +619,73 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     T = std::min(T, 512);
 
     long long M = q.M, K = q.K;
+    bool has_cb = (q.load_fn && *q.load_fn) || (q.store_fn && *q.store_fn);
+    // compile-time-size kernel, vectorised over M when the layout allows it
+    const ct_entry *ct = nullptr;
+    int V = 1;
+    if (!has_cb) {
+        int vw = vector_width(q.prec, rad);
+        bool v_ok = !q.force_v1 && vw > 1 && M % vw == 0 && q.is1 % vw == 0 && q.os1 % vw == 0 &&
+                    q.is2 % vw == 0 && q.os2 % vw == 0;
+        if (v_ok) {
+            ct = ct_lookup(q.prec, ps.kind, Nc, T, vw, rad.data(), L);
+            V = ct ? vw : 1;
+        }
+        if (!ct) {
+            ct = ct_lookup(q.prec, ps.kind, Nc, T, 1, rad.data(), L);
+        }
+    }
+    int const max_block = ct ? 256 : 512;
+    // the runtime kernel ping-pongs between two buffers when a stage goes shared->shared;
+    // compile-time kernels run their stages in place in one buffer
+    int nbuf = 1;
+    for (int s = 0; s < L && !ct; ++s) {
+        bool src_g = s == 0;
+        bool dst_g = s == L - 1 && !post;
+        if (!src_g && !dst_g) {
+            nbuf = 2;
+        }
+    }
+
     int Mb;
     if (q.Mb > 0) {
         Mb = static_cast<int>(std::min<long long>(q.Mb, M));
     } else if (M == 1) {
         Mb = 1;
-    } else if (is_real && M <= 64 && M * T <= 512) {
+    } else if (is_real && M <= 64 && (M / V) * T <= max_block) {
         Mb = static_cast<int>(M);
     } else {
         Mb = static_cast<int>(std::min<long long>(M, 32));
     }
-    while (Mb > 1 && Mb * T > 512) {
-        Mb = (Mb + 1) / 2;
+    while (Mb > V && (Mb / V) * T > max_block) {
+        Mb = std::max(V, (Mb / 2) / V * V);
     }
+    if (Mb % V != 0) {
+        Mb = std::max(V, Mb / V * V);
+    }
+    int const lanes_per_k = (Mb / V) * T;
     std::size_t celem = 2 * static_cast<std::size_t>(q.prec);
     // shared padding i -> i + (i >> shift) * add adds at most a quarter (choose_padding)
-    auto buf_elems = [&](int kb) {
-        long long last = static_cast<long long>(kb) * Nc * Mb - 1;
+    auto buf_elems = [&](int kb, int mb) {
+        long long last = static_cast<long long>(kb) * Nc * mb - 1;
         return last + (last >> 2) + 1;
     };
-    int Kb = q.Kb > 0 ? q.Kb : std::max(1, 256 / (Mb * T));
+    int Kb = q.Kb > 0 ? q.Kb : std::max(1, 256 / lanes_per_k);
     Kb = static_cast<int>(std::min<long long>(Kb, K));
     Kb = std::max(Kb, 1);
-    while (Kb * Mb * T > 512 && Kb > 1) {
+    while (Kb * lanes_per_k > max_block && Kb > 1) {
         Kb /= 2;
     }
     std::size_t const soft_limit = 96 * 1024;
-    while (Kb > 1 && nbuf * buf_elems(Kb) * celem > soft_limit) {
+    while (Kb > 1 && nbuf * buf_elems(Kb, Mb) * celem > soft_limit) {
         Kb /= 2;
     }
     // a tile of Mb transforms that does not fit is split along M (in-place real
     // transforms then become unsupported, as in the reference when Mb < M)
-    while (Mb > 1 && nbuf * buf_elems(Kb) * celem > soft_limit) {
-        Mb = (Mb + 1) / 2;
+    while (Mb > V && nbuf * buf_elems(Kb, Mb) * celem > soft_limit) {
+        Mb = std::max(V, (Mb / 2) / V * V);
     }
-    std::size_t smem = nbuf * buf_elems(Kb) * celem;
+    std::size_t smem = nbuf * buf_elems(Kb, Mb) * celem;
     if (smem > static_cast<std::size_t>(max_optin_smem(device))) {
         bad_config("FFT length " + std::to_string(N) + " needs " + std::to_string(smem) +
                    " bytes of shared memory per block, more than the device provides");
@@ -668,7 +715,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     p.flags = flags;
     p.nbuf = nbuf;
     p.scale = 1.0;
-    choose_padding(p, q.prec, post);
+    choose_padding(p, q.prec, post, V, ct != nullptr);
     {
         long long last = static_cast<long long>(Kb) * Nc * Mb - 1;
         p.buf_elems = static_cast<int>(last + (last >> p.pad_shift) * p.pad_add + 1);
@@ -686,7 +733,8 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         bad_config("tensor too large for one launch");
     }
     ps.grid = static_cast<unsigned>(p.m_tiles * k_tiles);
-    ps.block = static_cast<unsigned>(Mb * T * Kb);
+    ps.block = static_cast<unsigned>((Mb / V) * T * Kb);
+    ps.V = V;
     ps.smem = smem;
     ps.inplace_ok = !is_real || Mb >= M;
     ps.tw = get_twiddles(device, q.prec, Nt);
@@ -698,9 +746,8 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     for (int s = 0; s < L; ++s) {
         id << (s ? "x" : "") << rad[s];
     }
-    id << "_T" << T << "_Kb" << Kb << "_is" << q.is1 << "_" << q.is2 << "_os" << q.os1 << "_"
+    id << "_T" << T << "_V" << V << "_Kb" << Kb << "_is" << q.is1 << "_" << q.is2 << "_os" << q.os1 << "_"
        << q.os2;
-    bool has_cb = (q.load_fn && *q.load_fn) || (q.store_fn && *q.store_fn);
     if (q.load_fn && *q.load_fn) {
         id << "_" << q.load_fn;
     }
@@ -710,9 +757,13 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     ps.identifier = c_ident(id.str());
 
     if (!has_cb) {
-        const ct_entry *ct = ct_lookup(q.prec, ps.kind, Nc, T, rad.data(), L);
         ps.func = ct ? ct->fn : (q.prec == 4 ? kernel_f32(ps.kind) : kernel_f64(ps.kind));
         ps.specialized = ct != nullptr;
+        if (V > 1) {
+            pass_request q1 = q;
+            q1.force_v1 = true;
+            ps.scalar_alt = std::make_shared<pass>(make_1d_pass(q1, device, cache));
+        }
         if (!ps.func) {
             throw status_error(BBFFT_INTERNAL_ERROR, "kernel not found");
         }
@@ -974,10 +1025,16 @@ static void execute_impl(bbfft_plan_s &plan, const void *in, void *out, cudaStre
         GB_CUDA(cudaSetDevice(plan.device));
     }
     void *tmp = plan.tmp ? plan.tmp->ptr : out;
-    for (auto &ps : plan.passes) {
+    for (auto &pass0 : plan.passes) {
+        const void *pin = pass0.in_sel == 0 ? in : tmp;
+        void *pout = pass0.out_sel == 1 ? out : tmp;
+        pass const &ps = (pass0.V > 1 && ((reinterpret_cast<std::uintptr_t>(pin) |
+                                           reinterpret_cast<std::uintptr_t>(pout)) % 16))
+                             ? *pass0.scalar_alt
+                             : pass0;
         fft_params p = ps.p;
-        p.in = ps.in_sel == 0 ? in : tmp;
-        p.out = ps.out_sel == 1 ? out : tmp;
+        p.in = pin;
+        p.out = pout;
         // paired real accesses need pointers aligned to one complex element
         std::uintptr_t const align = 2 * static_cast<std::uintptr_t>(ps.prec);
         if (reinterpret_cast<std::uintptr_t>(p.in) % align) {
