@@ -80,6 +80,8 @@ class PlanInfo(ctypes.Structure):
         ('block_threads', ctypes.c_uint32),
         ('shared_bytes', ctypes.c_size_t),
         ('workspace_bytes', ctypes.c_size_t),
+        ('vector_width', ctypes.c_uint32),
+        ('specialized', ctypes.c_uint32),
     ]
 
 

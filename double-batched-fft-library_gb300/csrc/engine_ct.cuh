@@ -106,16 +106,41 @@ template <class R, int Kind, int NC, int TT, int V> struct ct_ctx {
     static constexpr int kind_v = Kind;
     static constexpr bool half = Kind == kind_r2c_half || Kind == kind_c2r_half;
     static constexpr int NN = half ? 2 * NC : NC; // logical length (odd kinds: N = NC)
+    // lane vectors of 16 bytes or more are stored as 16-byte chunks in NQ planes with an
+    // XOR swizzle; 8-byte elements (float, V = 1) use the padded linear layout
+    static constexpr bool LIN = sizeof(C) * V < 16;
+    static constexpr int NQ = LIN ? 1 : int(sizeof(C)) * V / 16;
+    static constexpr int PER = LIN ? 1 : 16 / int(sizeof(C)); // complex per chunk
     const fft_params &p;
     C *sm;
     long long ib, ob;
-    int sbase; // shared index of element 0 of this thread's first transform
+    int sbase; // LIN: shared index of element 0; else chunk index of element 0
     int pshift, padd;
     bool active;
 
-    __device__ __forceinline__ int sidx(int n) const {
+    __device__ __forceinline__ int sidx(int n) const { // LIN layout
         int i = sbase + n * p.Mb;
         return i + (i >> pshift) * padd;
+    }
+    __device__ __forceinline__ int chunk(int n) const { // plane layout
+        int c = sbase + n * (p.Mb / V);
+        return c ^ (((c >> p.sw_a) & p.sw_mask) << p.sw_b);
+    }
+    __device__ __forceinline__ void sload(int n, C *o) const {
+        if constexpr (LIN) {
+            ldv<V>(sm + sidx(n), o);
+        } else {
+            const int c = chunk(n);
+            sfor<0, NQ>([&](auto Q) { ldv<PER>(sm + (Q.value * p.plane_chunks + c) * PER, o + Q.value * PER); });
+        }
+    }
+    __device__ __forceinline__ void sstore(int n, const C *o) const {
+        if constexpr (LIN) {
+            stv<V>(sm + sidx(n), o);
+        } else {
+            const int c = chunk(n);
+            sfor<0, NQ>([&](auto Q) { stv<PER>(sm + (Q.value * p.plane_chunks + c) * PER, o + Q.value * PER); });
+        }
     }
 
     __device__ __forceinline__ C adj_r2c_weight(C v, int k) const {
@@ -275,7 +300,7 @@ __device__ __forceinline__ void ct_stage(const Ctx &c, int j) {
             } else {
                 sfor<0, P>([&](auto I) {
                     C t[V];
-                    ldv<V>(c.sm + c.sidx(b + I.value * nb), t);
+                    c.sload(b + I.value * nb, t);
                     sfor<0, V>([&](auto U) { v[it][U.value][I.value] = t[U.value]; });
                 });
             }
@@ -305,7 +330,7 @@ __device__ __forceinline__ void ct_stage(const Ctx &c, int j) {
                         c.gstore(o + I.value * NS, t);
                     }
                 } else {
-                    stv<V>(c.sm + c.sidx(o + I.value * NS), t);
+                    c.sstore(o + I.value * NS, t);
                 }
             });
         }
@@ -322,7 +347,7 @@ __device__ __forceinline__ void ct_r2c_post(const Ctx &c, int j) {
     R g0[V];
     if (c.p.flags & flag_adj_c2r) {
         C z0[V];
-        ldv<V>(c.sm + c.sidx(0), z0);
+        c.sload(0, z0);
         sfor<0, V>([&](auto U) { g0[U.value] = z0[U.value].x + z0[U.value].y; });
     }
 #pragma unroll
@@ -331,8 +356,8 @@ __device__ __forceinline__ void ct_r2c_post(const Ctx &c, int j) {
         if (cnt % TT == 0 || i < cnt) {
             const int io = NC - i;
             C y1[V], y2[V], xi[V], xo[V];
-            ldv<V>(c.sm + c.sidx(i), y1);
-            ldv<V>(c.sm + c.sidx(io == NC ? 0 : io), y2);
+            c.sload(i, y1);
+            c.sload(io == NC ? 0 : io, y2);
             C w = __ldg(tw + i);
             C iw = mk<R>(-w.y, w.x);
             sfor<0, V>([&](auto U) {
@@ -391,8 +416,9 @@ __device__ __forceinline__ void fft_tile_ct(const fft_params &p) {
     const int m_l = mv * V;
     const long long m = mt * p.Mb + m_l;
     const long long k = kt * p.Kb + k_l;
-    Ctx c{p, reinterpret_cast<cplx<R> *>(smem_raw), m + k * p.is2, m + k * p.os2,
-          k_l * NC * p.Mb + m_l, p.pad_shift, p.pad_add, (m < p.M) && (k < p.K)};
+    const int sbase = Ctx::LIN ? k_l * NC * p.Mb + m_l : k_l * NC * mvb + mv;
+    Ctx c{p, reinterpret_cast<cplx<R> *>(smem_raw), m + k * p.is2, m + k * p.os2, sbase,
+          p.pad_shift, p.pad_add, (m < p.M) && (k < p.K)};
     ct_run<Ctx, R, NC, TT, V, 0, sizeof...(Ps), 1, Ps...>(c, j);
 }
 

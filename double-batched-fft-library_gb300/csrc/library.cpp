@@ -433,114 +433,179 @@ static int vector_width(int prec, std::vector<int> const &rad) {
     return v;
 }
 
-// Shared-memory bank model: wavefronts needed by one warp request of 8-byte (complex
-// float) or 16-byte (complex double) elements; each wavefront serves 128 bytes and a bank
-// conflict occurs when two lanes of a wavefront touch different words of one bank.
-static int wavefronts(int const *elem, int lanes, int elem_bytes) {
-    int per = std::max(1, 128 / elem_bytes); // lanes served per wavefront without conflicts
-    int words = elem_bytes / 4;
-    int total = 0;
-    for (int g = 0; g < lanes; g += per) {
+// Shared-memory bank model.  One warp instruction in which every lane moves `w` bytes
+// (8 or 16) is served in wavefronts of 128 / w lanes; within a wavefront a bank serves one
+// 4-byte word at a time, so the cost of a wavefront is the largest number of distinct words
+// that its lanes touch in one bank.
+static long instr_cost(long const *addr, int w) {
+    int per = 128 / w;
+    long total = 0;
+    for (int g = 0; g < 32; g += per) {
         int worst = 1;
-        for (int bank = 0; bank < 32; ++bank) {
-            int distinct[32];
-            int nd = 0;
-            for (int l = g; l < g + per && l < lanes; ++l) {
-                if (elem[l] < 0) {
-                    continue;
-                }
-                for (int w = 0; w < words; ++w) {
-                    int word = elem[l] * words + w;
-                    if (word % 32 != bank) {
-                        continue;
-                    }
-                    bool seen = false;
-                    for (int d = 0; d < nd; ++d) {
-                        seen = seen || distinct[d] == word;
-                    }
-                    if (!seen && nd < 32) {
-                        distinct[nd++] = word;
-                    }
-                }
+        long words[32][8];
+        int nw[32] = {0};
+        for (int l = g; l < g + per; ++l) {
+            if (addr[l] < 0) {
+                continue;
             }
-            worst = std::max(worst, nd);
+            for (int k = 0; k < w / 4; ++k) {
+                long word = addr[l] / 4 + k;
+                int bank = static_cast<int>(word % 32);
+                bool seen = false;
+                for (int d = 0; d < nw[bank]; ++d) {
+                    seen = seen || words[bank][d] == word;
+                }
+                if (!seen && nw[bank] < 8) {
+                    words[bank][nw[bank]++] = word;
+                }
+                worst = std::max(worst, nw[bank]);
+            }
         }
         total += worst;
     }
     return total;
 }
 
-// Pick the shared-memory padding that minimises the modelled wavefronts of the first warp
-// over all shared accesses of the stages (Stockham reads/writes and the r2c post-process).
-void choose_padding(fft_params &p, int prec, bool post, int V, bool inplace_stages) {
-    static const int cands[][2] = {{4, 1}, {3, 1}, {5, 1}, {6, 8}, {5, 8}, {7, 8},
-                                   {4, 2}, {5, 2}, {6, 4}, {30, 0}};
-    // a lane moves V consecutive elements: the access is modelled as one element of V
-    // times the size; vectors must stay contiguous and 16-byte aligned after padding
-    int const eb = 2 * prec * V;
-    int const lanes = 32;
+struct layout_choice {
+    bool planes = false;
+    int sh = 30, ad = 0;          // linear: i -> i + (i >> sh) * ad
+    int a = 30, b = 0, mask = 0;  // planes: c -> c ^ (((c >> a) & mask) << b)
+};
+
+// Modelled cost of all shared accesses of the first warp of a tile (Stockham reads and
+// writes of every shared stage and the r2c post-process) under a layout.
+static long layout_cost(fft_params const &p, int prec, bool post, int V, layout_choice const &L) {
+    int const eb = 2 * prec;
     int const mvb = p.Mb / V;
-    int best = -1, best_cost = 1 << 30;
-    for (int ci = 0; ci < static_cast<int>(sizeof(cands) / sizeof(cands[0])); ++ci) {
-        int sh = cands[ci][0], ad = cands[ci][1];
-        if (V > 1 && ((1 << sh) < V || (prec == 4 && ad % 2 != 0))) {
-            continue;
+    int const nq = L.planes ? std::max(1, eb * V / 16) : 1;
+    int const w = L.planes ? 16 : eb * V; // bytes per lane per instruction (LIN: V * eb <= 16)
+    long const plane = 1L << 20;          // planes far apart: no interaction modelled
+    auto addr = [&](int k_l, int n, int mv, int q) -> long {
+        if (!L.planes) {
+            long i = (static_cast<long>(k_l) * p.Nc + n) * p.Mb + mv * V;
+            i = i + (i >> L.sh) * L.ad;
+            return i * eb;
         }
-        auto idx = [&](int k_l, int n, int m_l) {
-            int i = (k_l * p.Nc + n) * p.Mb + m_l;
-            return (i + (i >> sh) * ad) / V; // in units of the lane's vector
-        };
-        long cost = 0;
-        int Ns = 1;
-        (void)inplace_stages;
-        for (int s = 0; s < p.L; ++s) {
-            int P = p.radix[s];
-            bool src_g = s == 0;
-            bool dst_g = s == p.L - 1 && !post;
-            int nb = p.Nc / P;
-            for (int r = 0; r < P && r < 16; ++r) {
-                int rd[32], wr[32];
-                for (int l = 0; l < lanes; ++l) {
-                    int m_l = (l % mvb) * V, j = (l / mvb) % p.T, k_l = l / (mvb * p.T);
+        long c = (static_cast<long>(k_l) * p.Nc + n) * mvb + mv;
+        c = c ^ (((c >> L.a) & L.mask) << L.b);
+        return (q * plane + c) * 16;
+    };
+    long cost = 0;
+    int Ns = 1;
+    long rd[32], wr[32];
+    for (int s = 0; s < p.L; ++s) {
+        int P = p.radix[s];
+        bool src_g = s == 0;
+        bool dst_g = s == p.L - 1 && !post;
+        int nb = p.Nc / P;
+        for (int r = 0; r < P; ++r) {
+            for (int q = 0; q < nq; ++q) {
+                for (int l = 0; l < 32; ++l) {
+                    int mv = l % mvb, j = (l / mvb) % p.T, k_l = l / (mvb * p.T);
                     rd[l] = wr[l] = -1;
                     if (k_l >= p.Kb || j >= nb) {
                         continue;
                     }
-                    int b = j;
-                    int o = b + (b / Ns) * Ns * (P - 1);
-                    rd[l] = idx(k_l, b + r * nb, m_l);
-                    wr[l] = idx(k_l, o + r * Ns, m_l);
+                    int o = j + (j / Ns) * Ns * (P - 1);
+                    rd[l] = addr(k_l, j + r * nb, mv, q);
+                    wr[l] = addr(k_l, o + r * Ns, mv, q);
                 }
                 if (!src_g) {
-                    cost += wavefronts(rd, lanes, eb);
+                    cost += instr_cost(rd, w);
                 }
                 if (!dst_g) {
-                    cost += wavefronts(wr, lanes, eb);
+                    cost += instr_cost(wr, w);
                 }
             }
-            Ns *= P;
         }
-        if (post) {
-            int a[32], b2[32];
-            for (int l = 0; l < lanes; ++l) {
-                int m_l = (l % mvb) * V, j = (l / mvb) % p.T, k_l = l / (mvb * p.T);
-                a[l] = b2[l] = -1;
+        Ns *= P;
+    }
+    if (post) {
+        for (int q = 0; q < nq; ++q) {
+            for (int l = 0; l < 32; ++l) {
+                int mv = l % mvb, j = (l / mvb) % p.T, k_l = l / (mvb * p.T);
+                rd[l] = wr[l] = -1;
                 if (k_l >= p.Kb || 2 * j > p.Nc) {
                     continue;
                 }
-                a[l] = idx(k_l, j, m_l);
-                b2[l] = idx(k_l, (p.Nc - j) % p.Nc, m_l);
+                rd[l] = addr(k_l, j, mv, q);
+                wr[l] = addr(k_l, (p.Nc - j) % p.Nc, mv, q);
             }
-            cost += wavefronts(a, lanes, eb) + wavefronts(b2, lanes, eb);
-        }
-        // prefer less padding on ties (cands are ordered by preference)
-        if (cost < best_cost) {
-            best_cost = static_cast<int>(cost);
-            best = ci;
+            cost += instr_cost(rd, w) + instr_cost(wr, w);
         }
     }
-    p.pad_shift = cands[best][0];
-    p.pad_add = cands[best][1];
+    return cost;
+}
+
+// Pick the shared layout with the fewest modelled wavefronts; fills the layout fields of
+// p and returns the bytes of one buffer.
+std::size_t choose_layout(fft_params &p, int prec, bool post, int V, bool planes_kernel) {
+    int const eb = 2 * prec;
+    std::vector<layout_choice> cands;
+    if (!planes_kernel) {
+        static const int lin[][2] = {{30, 0}, {4, 1}, {3, 1}, {5, 1}, {6, 8}, {5, 8}, {7, 8},
+                                     {4, 2}, {5, 2}, {6, 4}};
+        for (auto const &c : lin) {
+            if (V > 1 && ((1 << c[0]) < V || (c[1] % V) != 0)) {
+                continue;
+            }
+            layout_choice L;
+            L.sh = c[0];
+            L.ad = c[1];
+            cands.push_back(L);
+        }
+    } else {
+        layout_choice none;
+        none.planes = true;
+        cands.push_back(none);
+        for (int a = 2; a <= 8; ++a) {
+            for (int b = 0; b <= 2; ++b) {
+                for (int bits = 1; bits <= 3; ++bits) {
+                    if (b + bits > a) {
+                        continue;
+                    }
+                    layout_choice L;
+                    L.planes = true;
+                    L.a = a;
+                    L.b = b;
+                    L.mask = (1 << bits) - 1;
+                    cands.push_back(L);
+                }
+            }
+        }
+    }
+    long best_cost = -1;
+    layout_choice best;
+    for (auto const &L : cands) {
+        long c = layout_cost(p, prec, post, V, L);
+        if (best_cost < 0 || c < best_cost) {
+            best_cost = c;
+            best = L;
+        }
+    }
+    p.pad_shift = best.sh;
+    p.pad_add = best.ad;
+    p.sw_a = best.a;
+    p.sw_b = best.b;
+    p.sw_mask = best.mask;
+    long const n = static_cast<long>(p.Kb) * p.Nc * p.Mb; // complex elements per buffer
+    if (!best.planes) {
+        long last = n - 1;
+        p.buf_elems = static_cast<int>(last + (last >> best.sh) * best.ad + 1);
+        p.plane_chunks = 0;
+        return static_cast<std::size_t>(p.buf_elems) * eb;
+    }
+    int nq = std::max(1, eb * V / 16);
+    long chunks = n * eb / nq / 16; // chunks per plane
+    int bits = 0;
+    while ((1 << bits) <= best.mask) {
+        ++bits;
+    }
+    long gran = 1L << (best.b + bits); // the swizzle permutes within aligned blocks of gran
+    chunks = (chunks + gran - 1) / gran * gran;
+    p.plane_chunks = static_cast<int>(chunks);
+    p.buf_elems = static_cast<int>(nq * chunks * 16 / eb);
+    return static_cast<std::size_t>(nq) * chunks * 16;
 }
 
 pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
@@ -715,12 +780,9 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     p.flags = flags;
     p.nbuf = nbuf;
     p.scale = 1.0;
-    choose_padding(p, q.prec, post, V, ct != nullptr);
-    {
-        long long last = static_cast<long long>(Kb) * Nc * Mb - 1;
-        p.buf_elems = static_cast<int>(last + (last >> p.pad_shift) * p.pad_add + 1);
-    }
-    smem = static_cast<std::size_t>(nbuf) * p.buf_elems * celem;
+    // compile-time kernels store lane vectors of 16 bytes or more as swizzled 16-byte planes
+    bool planes_kernel = ct != nullptr && celem * V >= 16;
+    smem = static_cast<std::size_t>(nbuf) * choose_layout(p, q.prec, post, V, planes_kernel);
     // paired real loads / stores: adjacent (unit N-stride, one transform per M) and aligned
     if (ps.kind == kind_r2c_half && q.is1 == 1 && M == 1 && q.is2 % 2 == 0) {
         p.flags |= flag_vec_in;
@@ -1328,6 +1390,8 @@ int bbfft_plan_get_info(bbfft_plan_t plan, bbfft_plan_info *info) {
         info->block_threads = ps.block;
         info->shared_bytes = ps.smem;
         info->workspace_bytes = plan->tmp ? plan->tmp->bytes : 0;
+        info->vector_width = static_cast<uint32_t>(ps.V);
+        info->specialized = ps.specialized ? 1u : 0u;
     });
 }
 

@@ -43,6 +43,9 @@ struct fft_params {
     int nbuf;              // shared buffers (1 or 2)
     int buf_elems;         // padded elements per buffer
     int pad_shift, pad_add; // shared index i -> i + (i >> pad_shift) * pad_add
+    // compile-time kernels with 16-byte lane vectors: 16-byte chunk c of plane q lives at
+    // q * plane_chunks + (c ^ (((c >> sw_a) & sw_mask) << sw_b))
+    int sw_a, sw_b, sw_mask, plane_chunks;
     double scale;          // used with flag_scale_out
 };
 

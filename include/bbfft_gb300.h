@@ -180,6 +180,8 @@ typedef struct bbfft_plan_info {
     uint32_t block_threads; /* threads per CTA of the first pass */
     size_t shared_bytes;    /* dynamic shared memory of the first pass */
     size_t workspace_bytes; /* device scratch owned by the plan (nd temporaries) */
+    uint32_t vector_width;  /* transforms per thread along M (first pass) */
+    uint32_t specialized;   /* 1 if the first pass runs a compile-time-size kernel */
 } bbfft_plan_info;
 BBFFT_GB300_API int bbfft_plan_get_info(bbfft_plan_t plan, bbfft_plan_info *info);
 
