@@ -1,0 +1,128 @@
+"""Autotuner for the double-batched FFT plans on GB300.
+
+For a 1d configuration the tuner times candidate blockings of the plan -- transforms per
+thread along M (V), the M- and K-extent of a CTA tile (Mb, Kb) -- with CUDA events on
+device-resident data and records the fastest in a tuning table.  bbfft_plan_create
+consults the table (one line per precision, kernel kind, N and M:
+``<prec> <kind> <N> <M> <V> <Mb> <Kb>``).  The radices and threads per transform stay
+those of the library's heuristic, which the compile-time kernels are instantiated for.
+
+Usage (on the GPU):  python -m bbfft_gb300.autotune [--out PATH] [--quick]
+"""
+import argparse
+import os
+import re
+import sys
+
+import bbfft_gb300 as bb
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DEFAULT_OUT = os.path.join(os.path.dirname(HERE), 'tuning', 'gb300.tune')
+
+SWEEP_N = [16, 32, 64, 128, 256, 512, 48, 96, 160, 224, 384, 7, 11, 13]
+
+
+def _tensor_elems(dim, shape, stride):
+    return sum((shape[d] - 1) * stride[d] for d in range(dim + 2)) + 1
+
+
+def tune_config(torch, prec, type, N, M, K, reps=4, verbose=False):
+    """Time every candidate blocking of one 1d configuration; returns (entry, results)."""
+    direction = bb.BACKWARD if type == bb.C2R else bb.FORWARD
+    cfg = bb.configuration(1, [M, N, K], precision=prec, type=type, direction=direction)
+    n_in = N // 2 + 1 if type == bb.C2R else N
+    n_out = N // 2 + 1 if type == bb.R2C else N
+    in_b = _tensor_elems(1, [M, n_in, K], list(cfg.istride)) * prec * (1 if type == bb.R2C else 2)
+    out_b = _tensor_elems(1, [M, n_out, K], list(cfg.ostride)) * prec * (1 if type == bb.C2R else 2)
+    x = torch.randn(in_b // 4 + 16, device='cuda')
+    y = torch.empty(out_b // 4 + 16, device='cuda')
+    stream = torch.cuda.current_stream()
+    results = {}
+    mbs = sorted({m for m in (M, 64, 32, 16, 8, 4, 2, 1) if m <= M and m <= 64}, reverse=True)
+    for V in (0, 1, 2, 4):
+        for Mb in mbs:
+            for Kb in (0, 1, 2, 4, 8, 16, 32, 64, 128, 256):
+                try:
+                    plan = bb.Plan(cfg, stream=stream.cuda_stream, tuning=(None, 0, V, Mb, Kb))
+                except bb.BBFFTError:
+                    continue
+                info = plan.info()
+                key = (info.vector_width, info.mb, info.kb)
+                if key in results:
+                    continue
+                for _ in range(2):
+                    plan.execute(x.data_ptr(), y.data_ptr())
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(reps):
+                    plan.execute(x.data_ptr(), y.data_ptr())
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1) / reps
+                results[key] = (ms, info.identifier.decode())
+                plan.destroy()
+    best_key = min(results, key=lambda k: results[k][0])
+    ident = results[best_key][1]
+    kind = re.match(r'gbfft_f\d+_([a-z0-9]+)_', ident).group(1)
+    nbytes = (n_in * (prec if type == bb.R2C else 2 * prec) + n_out * (prec if type == bb.C2R else 2 * prec)) * M * K
+    gbs = nbytes / (results[best_key][0] * 1e-3) / 1e9
+    entry = (prec, kind, N, M) + best_key
+    if verbose:
+        worst = max(r[0] for r in results.values())
+        print('prec %d type %d N %4d M %4d: best V=%d Mb=%d Kb=%d %.1f GB/s (%d candidates, worst %.2fx)'
+              % (prec, type, N, M, best_key[0], best_key[1], best_key[2], gbs, len(results),
+                 worst / results[best_key][0]), flush=True)
+    return entry, gbs
+
+
+def default_configs(quick=False):
+    """The configurations of the benchmark workloads."""
+    cfgs = []
+    for prec in (4, 8):
+        for N in SWEEP_N:
+            K = (1 << 30) // (prec * 8 * N)
+            if quick:
+                K = max(1, K // 8)
+            cfgs.append((prec, bb.R2C, N, 8, K))
+            cfgs.append((prec, bb.C2R, N, 8, K))
+    # c2c, M=1: the N=64 K=16384 case and the N in {64, 256, 512} K=2^20 cases
+    for N in (64, 256, 512):
+        cfgs.append((4, bb.C2C, N, 1, (1 << 20) if not quick else (1 << 17)))
+    # passes of the 2d 128x128 r2c (K=2048) and the 3d 64^3 c2c (K=64)
+    cfgs.append((4, bb.R2C, 128, 1, 128 * 2048))
+    cfgs.append((4, bb.C2C, 128, 65, 2048))
+    cfgs.append((4, bb.C2R, 128, 1, 128 * 2048))
+    cfgs.append((4, bb.C2C, 64, 1, 64 * 64 * 64))
+    cfgs.append((4, bb.C2C, 64, 64, 64 * 64))
+    cfgs.append((4, bb.C2C, 64, 4096, 64))
+    return cfgs
+
+
+def write_table(path, entries):
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    lines = ['# bbfft GB300 tuning table: <prec bytes> <kind> <N> <M> <V> <Mb> <Kb>  # GB/s',
+             '# written by bbfft_gb300/autotune.py from CUDA-event timings on a GB300']
+    for e, gbs in entries:
+        lines.append('%d %s %d %d %d %d %d  # %.1f' % (e + (gbs,)))
+    with open(path, 'w') as f:
+        f.write('\n'.join(lines) + '\n')
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--out', default=DEFAULT_OUT)
+    ap.add_argument('--quick', action='store_true')
+    args = ap.parse_args(argv)
+    import torch
+
+    os.environ['BBFFT_GB300_TUNING'] = 'off'  # candidates are set explicitly
+    entries = []
+    for prec, type, N, M, K in default_configs(args.quick):
+        entries.append(tune_config(torch, prec, type, N, M, K, verbose=True))
+    write_table(args.out, entries)
+    print('wrote', args.out)
+
+
+if __name__ == '__main__':
+    sys.exit(main())

@@ -14,13 +14,16 @@
 #include "params.h"
 
 #include <cuda_runtime.h>
+#include <dlfcn.h>
 #include <nvrtc.h>
 
 #include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -362,8 +365,57 @@ struct pass_request {
     // tuning overrides
     std::vector<int> radices;
     int T = 0, Mb = 0, Kb = 0;
+    int V = 0; // 0: automatic, 1: no vectorisation along M, > 1: requested width
     bool force_v1 = false;
 };
+
+// ------------------------------------------------------------------------------------------
+// tuning table written by the autotuner (bbfft_gb300/autotune.py): one line per
+//   <prec bytes> <kind> <N> <M or -1> <V> <Mb> <Kb>
+// chosen by timing candidate blockings on the device.  Loaded once from
+// $BBFFT_GB300_TUNING ("off" disables) or <package>/tuning/gb300.tune.
+
+struct tune_entry {
+    int V, Mb, Kb;
+};
+
+static std::string library_dir() {
+    Dl_info info;
+    if (dladdr(reinterpret_cast<void *>(&library_dir), &info) && info.dli_fname) {
+        std::string f = info.dli_fname;
+        auto pos = f.rfind('/');
+        return pos == std::string::npos ? std::string(".") : f.substr(0, pos);
+    }
+    return ".";
+}
+
+static std::map<std::tuple<int, std::string, int, long long>, tune_entry> const &tuning_table() {
+    static std::map<std::tuple<int, std::string, int, long long>, tune_entry> table;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        const char *env = std::getenv("BBFFT_GB300_TUNING");
+        std::string path = env ? env : library_dir() + "/../../tuning/gb300.tune";
+        if (path == "off") {
+            return;
+        }
+        std::ifstream in(path);
+        std::string line;
+        while (std::getline(in, line)) {
+            auto hash = line.find('#');
+            if (hash != std::string::npos) {
+                line = line.substr(0, hash);
+            }
+            std::istringstream ls(line);
+            int prec, N, V, Mb, Kb;
+            long long M;
+            std::string kind;
+            if (ls >> prec >> kind >> N >> M >> V >> Mb >> Kb) {
+                table[std::make_tuple(prec, kind, N, M)] = tune_entry{V, Mb, Kb};
+            }
+        }
+    });
+    return table;
+}
 
 static int max_optin_smem(int device) {
     int v = 0;
@@ -402,6 +454,17 @@ static uint64_t fnv1a(const char *data, std::size_t n) {
         h *= 1099511628211ull;
     }
     return h;
+}
+
+static char const *kind_name(int kind);
+
+static tune_entry const *find_tuning(int prec, int kind, int N, long long M) {
+    auto const &t = tuning_table();
+    auto it = t.find(std::make_tuple(prec, std::string(kind_name(kind)), N, M));
+    if (it == t.end()) {
+        it = t.find(std::make_tuple(prec, std::string(kind_name(kind)), N, -1LL));
+    }
+    return it == t.end() ? nullptr : &it->second;
 }
 
 static char const *kind_name(int kind) {
@@ -685,11 +748,22 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
 
     long long M = q.M, K = q.K;
     bool has_cb = (q.load_fn && *q.load_fn) || (q.store_fn && *q.store_fn);
+    int reqV = q.V, reqMb = q.Mb, reqKb = q.Kb;
+    if (q.radices.empty() && q.T == 0 && q.V == 0 && q.Mb == 0 && q.Kb == 0 && !q.force_v1) {
+        if (auto te = find_tuning(q.prec, ps.kind, N, M)) {
+            reqV = te->V;
+            reqMb = te->Mb;
+            reqKb = te->Kb;
+        }
+    }
     // compile-time-size kernel, vectorised over M when the layout allows it
     const ct_entry *ct = nullptr;
     int V = 1;
     if (!has_cb) {
         int vw = vector_width(q.prec, rad);
+        if (reqV > 0) {
+            vw = std::min(vw, reqV);
+        }
         bool v_ok = !q.force_v1 && vw > 1 && M % vw == 0 && q.is1 % vw == 0 && q.os1 % vw == 0 &&
                     q.is2 % vw == 0 && q.os2 % vw == 0;
         if (v_ok) {
@@ -713,8 +787,8 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     }
 
     int Mb;
-    if (q.Mb > 0) {
-        Mb = static_cast<int>(std::min<long long>(q.Mb, M));
+    if (reqMb > 0) {
+        Mb = static_cast<int>(std::min<long long>(reqMb, M));
     } else if (M == 1) {
         Mb = 1;
     } else if (is_real && M <= 64 && (M / V) * T <= max_block) {
@@ -735,7 +809,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         long long last = static_cast<long long>(kb) * Nc * mb - 1;
         return last + (last >> 2) + 1;
     };
-    int Kb = q.Kb > 0 ? q.Kb : std::max(1, 256 / lanes_per_k);
+    int Kb = reqKb > 0 ? reqKb : std::max(1, 256 / lanes_per_k);
     Kb = static_cast<int>(std::min<long long>(Kb, K));
     Kb = std::max(Kb, 1);
     while (Kb * lanes_per_k > max_block && Kb > 1) {
@@ -824,6 +898,8 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         if (V > 1) {
             pass_request q1 = q;
             q1.force_v1 = true;
+            q1.Mb = Mb;
+            q1.Kb = std::max(1, Kb / V);
             ps.scalar_alt = std::make_shared<pass>(make_1d_pass(q1, device, cache));
         }
         if (!ps.func) {
@@ -1306,8 +1382,8 @@ int bbfft_plan_create_adjoint(const bbfft_configuration *cfg, cudaStream_t strea
 
 int bbfft_plan_create_tuned(const bbfft_configuration *cfg, cudaStream_t stream,
                             const uint32_t *radices, uint32_t num_radices,
-                            uint32_t threads_per_transform, uint32_t mb, uint32_t kb,
-                            bbfft_plan_t *plan) {
+                            uint32_t threads_per_transform, uint32_t vector_width, uint32_t mb,
+                            uint32_t kb, bbfft_plan_t *plan) {
     gbfft::pass_request t{};
     if (radices) {
         for (uint32_t i = 0; i < num_radices && radices[i] != 0; ++i) {
@@ -1315,6 +1391,8 @@ int bbfft_plan_create_tuned(const bbfft_configuration *cfg, cudaStream_t stream,
         }
     }
     t.T = static_cast<int>(threads_per_transform);
+    t.V = static_cast<int>(vector_width);
+    t.force_v1 = vector_width == 1;
     t.Mb = static_cast<int>(mb);
     t.Kb = static_cast<int>(kb);
     if (cfg && cfg->dim != 1) {

@@ -185,13 +185,17 @@ typedef struct bbfft_plan_info {
 } bbfft_plan_info;
 BBFFT_GB300_API int bbfft_plan_get_info(bbfft_plan_t plan, bbfft_plan_info *info);
 
-/* Override the automatic blocking of a 1d plan (autotuner hook; no counterpart).
- * radices: list of radices whose product is the complex FFT length; 0-terminated or
- * num_radices long.  threads_per_transform, mb, kb: 0 = automatic. */
+/* Override the automatic blocking of a 1d plan (autotuner hook; no counterpart in the
+ * reference).  radices: list whose product is the complex FFT length (NULL / 0 entries =
+ * automatic); threads_per_transform, mb, kb: 0 = automatic; vector_width: transforms per
+ * thread along M (0 = automatic, 1 = none).  Plans made with bbfft_plan_create consult the
+ * tuning table (BBFFT_GB300_TUNING or the package's tuning/gb300.tune) written by the
+ * autotuner. */
 BBFFT_GB300_API int bbfft_plan_create_tuned(const bbfft_configuration *cfg, cudaStream_t stream,
                                             const uint32_t *radices, uint32_t num_radices,
-                                            uint32_t threads_per_transform, uint32_t mb,
-                                            uint32_t kb, bbfft_plan_t *plan);
+                                            uint32_t threads_per_transform,
+                                            uint32_t vector_width, uint32_t mb, uint32_t kb,
+                                            bbfft_plan_t *plan);
 
 /* Thread-local message of the last failure (empty string if none). */
 BBFFT_GB300_API const char *bbfft_last_error(void);
