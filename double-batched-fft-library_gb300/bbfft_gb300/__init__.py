@@ -121,6 +121,8 @@ _SIGNATURES = {
     'bbfft_plan_retain': (ctypes.c_int, [_vp]),
     'bbfft_plan_destroy': (ctypes.c_int, [_vp]),
     'bbfft_plan_get_info': (ctypes.c_int, [_vp, ctypes.POINTER(PlanInfo)]),
+    'bbfft_c2r_2d_noalloc_f32': (ctypes.c_int, [_vp, _vp, ctypes.c_size_t, ctypes.c_size_t,
+                                                ctypes.c_size_t, ctypes.c_size_t, _vp]),
     'bbfft_last_error': (ctypes.c_char_p, []),
     'bbfft_version': (ctypes.c_char_p, []),
 }
@@ -306,6 +308,11 @@ def make_plan(cfg, stream=None, cache=None):
 
 def make_adjoint_plan(cfg, stream=None, cache=None):
     return Plan(cfg, stream=stream, cache=cache, adjoint=True)
+
+
+def c2r_2d_noalloc_f32(inp, out, M, N1, N2, K, stream=None):
+    """Allocation-free 2d c2r (include/bbfft_gb300.h: bbfft_c2r_2d_noalloc_f32)."""
+    _check(lib().bbfft_c2r_2d_noalloc_f32(int(inp), int(out), M, N1, N2, K, _stream_ptr(stream)))
 
 
 def version():

@@ -42,6 +42,15 @@ namespace gbfft {
 // errors
 
 thread_local std::string tl_error;
+// fixed-size message buffer for the allocation-free entry point (no string allocation)
+thread_local char tl_fixed_error[256];
+thread_local bool tl_fixed_active = false;
+void set_fixed_error(const char *msg) {
+    std::strncpy(tl_fixed_error, msg, sizeof(tl_fixed_error) - 1);
+    tl_fixed_error[sizeof(tl_fixed_error) - 1] = '\0';
+    tl_fixed_active = true;
+}
+void clear_fixed_error() { tl_fixed_active = false; }
 
 #define GB_CUDA(call)                                                                            \
     do {                                                                                         \
@@ -61,6 +70,7 @@ template <class F> int guarded(F &&f) {
         f();
         return BBFFT_SUCCESS;
     } catch (status_error const &e) {
+        tl_fixed_active = false;
         tl_error = e.what();
         return e.status();
     } catch (std::bad_alloc const &) {
@@ -264,74 +274,78 @@ std::shared_ptr<module> nvrtc_build(std::string const &source, std::string const
 
 static bool unrolled(int P) { return P == 1 || (P >= 2 && P <= 13) || P == 16; }
 
-static std::vector<int> prime_factors(int n) {
-    std::vector<int> f;
-    for (int p = 2; n > 1;) {
-        if (n % p == 0) {
-            f.push_back(p);
-            n /= p;
-        } else {
-            ++p;
-        }
-    }
-    return f;
-}
-
 // Radices for an Nc-point complex FFT: few stages, unrolled butterflies where possible.
-std::vector<int> choose_radices(int Nc) {
+// Writes at most 32 radices to `out` and returns their number (no allocation).
+int choose_radices_core(int Nc, int *out) {
     if (Nc == 1) {
-        return {1};
+        out[0] = 1;
+        return 1;
     }
-    auto f = prime_factors(Nc);
-    int c2 = 0, c3 = 0;
-    std::vector<int> odd, big;
-    for (int p : f) {
-        if (p == 2) {
-            ++c2;
-        } else if (p == 3) {
-            ++c3;
-        } else if (p <= 13) {
-            odd.push_back(p);
+    int c2 = 0, c3 = 0, nodd = 0, nbig = 0;
+    int odd[32], big[32];
+    for (int n = Nc, f = 2; n > 1;) {
+        if (n % f == 0) {
+            if (f == 2) {
+                ++c2;
+            } else if (f == 3) {
+                ++c3;
+            } else if (f <= 13) {
+                odd[nodd++] = f;
+            } else {
+                big[nbig++] = f;
+            }
+            n /= f;
         } else {
-            big.push_back(p);
+            ++f;
         }
     }
-    std::vector<int> r;
+    int r[32];
+    int nr = 0;
     while (c3 >= 2) {
-        r.push_back(9);
+        r[nr++] = 9;
         c3 -= 2;
     }
     if (c3 == 1) {
         if (c2 >= 2 && c2 != 3 && c2 != 6) { // keep 8 / 8x8 for the power-of-two part
-            r.push_back(12);
+            r[nr++] = 12;
             c2 -= 2;
         } else if (c2 >= 1) {
-            r.push_back(6);
+            r[nr++] = 6;
             c2 -= 1;
         } else {
-            r.push_back(3);
+            r[nr++] = 3;
         }
     }
-    for (int p : odd) {
-        if (p == 5 && c2 >= 1 && c2 % 3 == 1) {
-            r.push_back(10);
+    for (int i = 0; i < nodd; ++i) {
+        if (odd[i] == 5 && c2 >= 1 && c2 % 3 == 1) {
+            r[nr++] = 10;
             c2 -= 1;
         } else {
-            r.push_back(p);
+            r[nr++] = odd[i];
         }
     }
     if (c2 > 0) {
         int chunks = (c2 + 3) / 4;
         for (int i = 0; i < chunks; ++i) {
             int bits = c2 / chunks + (i < c2 % chunks ? 1 : 0);
-            r.push_back(1 << bits);
+            r[nr++] = 1 << bits;
         }
     }
-    std::sort(r.begin(), r.end(), [](int a, int b) { return a > b; });
-    for (int p : big) {
-        r.push_back(p); // generic radices last: they need a shared-memory source
+    std::sort(r, r + nr, [](int x, int y) { return x > y; });
+    int n = 0;
+    for (int i = 0; i < nr; ++i) {
+        out[n++] = r[i];
     }
-    return r;
+    for (int i = 0; i < nbig; ++i) {
+        out[n++] = big[i]; // generic radices last: they need a shared-memory source
+    }
+    return n;
+}
+
+std::vector<int> choose_radices(int Nc) {
+    int r[32];
+    int n = choose_radices_core(Nc, r);
+    return std::vector<int>(r, r + n);
 }
 
 struct pass {
@@ -963,6 +977,136 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     return ps;
 }
 
+// Launch geometry of one 1d pass computed without any allocation: heuristic radices and
+// blocking, one transform per thread along M, compile-time kernel when one exists, padded
+// linear shared layout.  The caller provides the twiddle table.  Returns an empty string
+// on success, else the reason the pass is not supported this way.
+const char *plan_pass_fixed(int prec, int type, int dir, long long M, long long N, long long K,
+                            long long is1, long long is2, long long os1, long long os2,
+                            int device, fft_params &p, unsigned &grid, unsigned &block,
+                            std::size_t &smem, const void *&func) {
+    bool is_real = type != BBFFT_C2C;
+    bool even = N % 2 == 0;
+    int kind = type == BBFFT_C2C ? kind_c2c
+               : type == BBFFT_R2C ? (even ? kind_r2c_half : kind_r2c_full)
+                                   : (even ? kind_c2r_half : kind_c2r_full);
+    int flags = (type == BBFFT_C2C && dir == BBFFT_BACKWARD) ? (flag_conj_in | flag_conj_out) : 0;
+    int Nc = static_cast<int>((is_real && even) ? N / 2 : N);
+    int Nt = (is_real && even) ? static_cast<int>(N) : Nc;
+    int rad[max_stages + 2];
+    int r0[32];
+    int n0 = choose_radices_core(Nc, r0);
+    int L = 0;
+    if (!unrolled(r0[0])) {
+        rad[L++] = 1;
+    }
+    for (int i = 0; i < n0; ++i) {
+        if (L >= max_stages) {
+            return "too many stages";
+        }
+        rad[L++] = r0[i];
+    }
+    bool post = kind == kind_r2c_half;
+    if (is_real && !post && L == 1) {
+        rad[L++] = 1;
+    }
+    if (L > max_stages) {
+        return "too many stages";
+    }
+    int pu = 1;
+    for (int i = 0; i < L; ++i) {
+        if (unrolled(rad[i])) {
+            pu = std::max(pu, rad[i]);
+        }
+    }
+    int T = pu == 1 ? std::min(Nc, 64) : std::max(1, Nc / pu);
+    T = std::min(T, 512);
+    const ct_entry *ct = ct_lookup(prec, kind, Nc, T, 1, rad, L);
+    int const max_block = ct ? 256 : 512;
+    int nbuf = 1;
+    for (int s2 = 0; s2 < L && !ct; ++s2) {
+        if (s2 != 0 && !(s2 == L - 1 && !post)) {
+            nbuf = 2;
+        }
+    }
+    int Mb = M == 1 ? 1 : static_cast<int>(std::min<long long>(M, 32));
+    while (Mb > 1 && Mb * T > max_block) {
+        Mb /= 2;
+    }
+    std::size_t celem = 2 * static_cast<std::size_t>(prec);
+    auto bytes = [&](int kb) {
+        long long last = static_cast<long long>(kb) * Nc * Mb - 1;
+        return static_cast<std::size_t>(nbuf) * static_cast<std::size_t>(last + (last >> 2) + 1) * celem;
+    };
+    int Kb = static_cast<int>(std::max<long long>(1, std::min<long long>(256 / (Mb * T), K)));
+    while (Kb > 1 && (Kb * Mb * T > max_block || bytes(Kb) > 96 * 1024)) {
+        Kb /= 2;
+    }
+    if ((N + 1) * std::max(std::llabs(is1), std::llabs(os1)) > 0x7fffffffLL) {
+        return "stride of the FFT mode too large";
+    }
+    p = fft_params{};
+    p.M = M;
+    p.K = K;
+    p.is1 = static_cast<int>(is1);
+    p.is2 = is2;
+    p.os1 = static_cast<int>(os1);
+    p.os2 = os2;
+    p.N = static_cast<int>(N);
+    p.Nc = Nc;
+    p.Nt = Nt;
+    p.L = L;
+    for (int i = 0; i < L; ++i) {
+        p.radix[i] = rad[i];
+    }
+    p.T = T;
+    p.Mb = Mb;
+    p.Kb = Kb;
+    p.m_tiles = static_cast<int>((M + Mb - 1) / Mb);
+    p.flags = flags;
+    p.nbuf = nbuf;
+    p.scale = 1.0;
+    static const int lin[][2] = {{30, 0}, {4, 1}, {3, 1}, {5, 1}, {6, 8}, {5, 8}, {7, 8},
+                                 {4, 2}, {5, 2}, {6, 4}};
+    long best_cost = -1;
+    layout_choice best;
+    for (auto const &c : lin) {
+        layout_choice Lc;
+        Lc.sh = c[0];
+        Lc.ad = c[1];
+        long cost = layout_cost(p, prec, post, 1, Lc);
+        if (best_cost < 0 || cost < best_cost) {
+            best_cost = cost;
+            best = Lc;
+        }
+    }
+    p.pad_shift = best.sh;
+    p.pad_add = best.ad;
+    p.sw_a = 30;
+    long long last = static_cast<long long>(Kb) * Nc * Mb - 1;
+    p.buf_elems = static_cast<int>(last + (last >> best.sh) * best.ad + 1);
+    smem = static_cast<std::size_t>(nbuf) * p.buf_elems * celem;
+    int optin = 0;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) {
+        return "cudaDeviceGetAttribute failed";
+    }
+    if (smem > static_cast<std::size_t>(optin)) {
+        return "FFT length needs more shared memory than the device provides";
+    }
+    long long k_tiles = (K + Kb - 1) / Kb;
+    if (static_cast<long long>(p.m_tiles) * k_tiles > 0x7fffffffLL) {
+        return "tensor too large for one launch";
+    }
+    grid = static_cast<unsigned>(p.m_tiles * k_tiles);
+    block = static_cast<unsigned>(Mb * T * Kb);
+    func = ct ? ct->fn : (prec == 4 ? kernel_f32(kind) : kernel_f64(kind));
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
+        return "cudaFuncSetAttribute failed";
+    }
+    return "";
+}
+
 } // namespace gbfft
 
 // ------------------------------------------------------------------------------------------
@@ -1206,7 +1350,9 @@ using gbfft::status_error;
 
 extern "C" {
 
-const char *bbfft_last_error(void) { return gbfft::tl_error.c_str(); }
+const char *bbfft_last_error(void) {
+    return gbfft::tl_fixed_active ? gbfft::tl_fixed_error : gbfft::tl_error.c_str();
+}
 const char *bbfft_version(void) { return "bbfft-gb300 0.1.0 (sm_103a)"; }
 
 int bbfft_default_istride(uint32_t dim, const size_t shape[BBFFT_MAX_TENSOR_DIM], int32_t type,

@@ -197,6 +197,21 @@ BBFFT_GB300_API int bbfft_plan_create_tuned(const bbfft_configuration *cfg, cuda
                                             uint32_t vector_width, uint32_t mb, uint32_t kb,
                                             bbfft_plan_t *plan);
 
+/* Allocation-free 2d c2r, float precision.  No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory when they transform (during CUDA graph
+ * capture, under allocators that forbid cudaMalloc, or with a fixed device footprint).
+ * Same result as a plan of {dim 2, shape {M, N1, N2, K}, f32, backward, c2r} with the
+ * default out-of-place layout, but the temporary between the two passes and the
+ * twiddle tables live in static device arrays of the library (16 MiB + 8 KiB held on
+ * every GPU that loads the library until the process exits).  Limits: N1, N2 <= 512 and
+ * M * (N1/2+1) * N2 * K <= 2^21; larger problems return BBFFT_BAD_CONFIGURATION.  It
+ * calls no cudaMalloc, cudaFree or other allocating routine.  The first call on a device
+ * resolves the device addresses of the static arrays.  All calls share the arrays, so
+ * calls that may overlap on the GPU (different streams, different host threads) race;
+ * serialise them.  Out-of-place only (in != out). */
+BBFFT_GB300_API int bbfft_c2r_2d_noalloc_f32(const void *in, void *out, size_t M, size_t N1,
+                                             size_t N2, size_t K, cudaStream_t stream);
+
 /* Thread-local message of the last failure (empty string if none). */
 BBFFT_GB300_API const char *bbfft_last_error(void);
 /* Library version string. */
