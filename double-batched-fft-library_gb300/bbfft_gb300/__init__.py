@@ -103,6 +103,10 @@ _SIGNATURES = {
     'bbfft_aot_cache_register_module': (ctypes.c_int, [_vp, _vp, ctypes.c_size_t,
                                                        ctypes.POINTER(ctypes.c_char_p),
                                                        ctypes.c_size_t, ctypes.c_int]),
+    'bbfft_aot_generate': (ctypes.c_int, [ctypes.POINTER(Configuration), ctypes.c_size_t, _vp,
+                                          ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t),
+                                          ctypes.c_char_p, ctypes.c_size_t,
+                                          ctypes.POINTER(ctypes.c_size_t)]),
     'bbfft_cache_destroy': (ctypes.c_int, [_vp]),
     'bbfft_cache_kernel_names': (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_size_t,
                                                 ctypes.POINTER(ctypes.c_size_t)]),
@@ -214,6 +218,17 @@ def parse_fft_descriptor(desc):
     cfg = Configuration()
     _check(lib().bbfft_parse_fft_descriptor(desc.encode(), ctypes.byref(cfg)))
     return cfg
+
+
+def aot_generate(cfgs, max_image=64 << 20):
+    """Compile the callback kernels of `cfgs` into one cubin; returns (image bytes, names)."""
+    arr = (Configuration * len(cfgs))(*cfgs)
+    buf = ctypes.create_string_buffer(max_image)
+    need = ctypes.c_size_t()
+    names = ctypes.create_string_buffer(8192)
+    _check(lib().bbfft_aot_generate(arr, len(cfgs), ctypes.cast(buf, _vp), max_image,
+                                    ctypes.byref(need), names, 8192, None))
+    return buf.raw[:need.value], [n for n in names.value.decode().split('\n') if n]
 
 
 class Cache:

@@ -239,16 +239,28 @@ static std::string nvrtc_arch(int device) {
     return "--gpu-architecture=" + arch;
 }
 
+std::vector<char> nvrtc_compile(std::string const &source, std::string const &name, int device);
+
 std::shared_ptr<module> nvrtc_build(std::string const &source, std::string const &name,
                                     int device) {
+    std::vector<char> cubin = nvrtc_compile(source, name, device);
+    auto m = std::make_shared<module>();
+    GB_CUDA(cudaLibraryLoadData(&m->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
+    return m;
+}
+
+std::vector<char> nvrtc_compile(std::string const &source, std::string const &name, int device) {
     nvrtcProgram prog;
     if (nvrtcCreateProgram(&prog, source.c_str(), (name + ".cu").c_str(), 0, nullptr, nullptr) !=
         NVRTC_SUCCESS) {
         throw status_error(BBFFT_COMPILE_ERROR, "nvrtcCreateProgram failed");
     }
     std::string arch = nvrtc_arch(device);
-    const char *opts[] = {arch.c_str(), "-std=c++17", "-lineinfo", "-DGBFFT_JIT=1"};
-    nvrtcResult rc = nvrtcCompileProgram(prog, 4, opts);
+    // -default-device: user callbacks may be written without __device__, like the
+    // reference's OpenCL-C functions
+    const char *opts[] = {arch.c_str(), "-std=c++17", "-lineinfo", "-default-device",
+                          "-DGBFFT_JIT=1"};
+    nvrtcResult rc = nvrtcCompileProgram(prog, 5, opts);
     std::size_t log_size = 0;
     nvrtcGetProgramLogSize(prog, &log_size);
     std::string log(log_size, '\0');
@@ -264,9 +276,7 @@ std::shared_ptr<module> nvrtc_build(std::string const &source, std::string const
     std::vector<char> cubin(cubin_size);
     nvrtcGetCUBIN(prog, cubin.data());
     nvrtcDestroyProgram(&prog);
-    auto m = std::make_shared<module>();
-    GB_CUDA(cudaLibraryLoadData(&m->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
-    return m;
+    return cubin;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -685,6 +695,52 @@ std::size_t choose_layout(fft_params &p, int prec, bool post, int V, bool planes
     return static_cast<std::size_t>(nq) * chunks * 16;
 }
 
+// Name of the callback kernel: the compiled code depends on the precision, the kernel kind
+// and the user module only, so plans of different shapes share one module.
+std::string callback_kernel_name(int prec, int kind, const char *src, std::size_t len,
+                                 const char *load_fn, const char *store_fn) {
+    std::ostringstream key;
+    key << "gbfft_cb_f" << prec * 8 << "_" << kind_name(kind) << "_" << (load_fn ? load_fn : "")
+        << "_" << (store_fn ? store_fn : "") << "_" << std::hex << fnv1a(src, len);
+    return c_ident(key.str());
+}
+
+// NVRTC program: the engine, the user module and one kernel per (name, precision, kind).
+// The user's load / store functions are called with the element offset of the tensor
+// (reference callback_accessor, src/base/generator/tensor_accessor.cpp:34-55).
+std::string callback_program(const char *cb, std::size_t len, const char *load_fn,
+                             const char *store_fn,
+                             std::vector<std::tuple<std::string, int, int>> const &kernels) {
+    std::ostringstream src;
+    src << "typedef decltype(sizeof(0)) size_t;\n";
+    src << kEngineSource << "\n";
+    src << std::string(cb, len) << "\n";
+    src << "struct gbfft_user_io {\n"
+        << "  static constexpr bool direct = false;\n"
+        << "  template <class T> static __device__ __forceinline__ T load(const T *t, long long "
+           "base, int off) {\n";
+    if (load_fn && *load_fn) {
+        src << "    return " << load_fn << "(const_cast<T *>(t), (size_t)(base + off));\n";
+    } else {
+        src << "    return (t + base)[off];\n";
+    }
+    src << "  }\n  template <class T> static __device__ __forceinline__ void store(T *t, long long "
+           "base, int off, T v) {\n";
+    if (store_fn && *store_fn) {
+        src << "    " << store_fn << "(t, (size_t)(base + off), v);\n";
+    } else {
+        src << "    (t + base)[off] = v;\n";
+    }
+    src << "  }\n};\n";
+    for (auto const &k : kernels) {
+        src << "extern \"C\" __global__ void __launch_bounds__(512) " << std::get<0>(k)
+            << "(const __grid_constant__ gbfft::fft_params p) {\n"
+            << "  gbfft::fft_tile<" << (std::get<1>(k) == 4 ? "float" : "double") << ", "
+            << std::get<2>(k) << ", gbfft_user_io>(p);\n}\n";
+    }
+    return src.str();
+}
+
 pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     pass ps;
     ps.prec = q.prec;
@@ -923,43 +979,16 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         if (!q.cb_source || q.cb_length == 0) {
             bad_config("callback function named but no callback source given");
         }
-        // The compiled code depends on precision, kind and the callbacks only, so modules
-        // are shared between plans of different shapes.
-        std::ostringstream key;
-        key << "gbfft_cb_f" << q.prec * 8 << "_" << kind_name(ps.kind) << "_"
-            << (q.load_fn ? q.load_fn : "") << "_" << (q.store_fn ? q.store_fn : "") << "_"
-            << std::hex << fnv1a(q.cb_source, q.cb_length);
-        std::string kname = c_ident(key.str());
+        std::string kname = callback_kernel_name(q.prec, ps.kind, q.cb_source, q.cb_length,
+                                                 q.load_fn, q.store_fn);
         std::shared_ptr<module> mod;
         if (cache) {
             mod = cache->get(kname, device);
         }
         if (!mod) {
-            std::ostringstream src;
-            src << "typedef decltype(sizeof(0)) size_t;\n";
-            src << kEngineSource << "\n";
-            src << std::string(q.cb_source, q.cb_length) << "\n";
-            src << "struct gbfft_user_io {\n"
-                << "  template <class T> static __device__ __forceinline__ T load(const T *p, "
-                   "unsigned long long off) {\n";
-            if (q.load_fn && *q.load_fn) {
-                src << "    return " << q.load_fn << "(const_cast<T *>(p), (size_t)off);\n";
-            } else {
-                src << "    return p[off];\n";
-            }
-            src << "  }\n  template <class T> static __device__ __forceinline__ void store(T *p, "
-                   "unsigned long long off, T v) {\n";
-            if (q.store_fn && *q.store_fn) {
-                src << "    " << q.store_fn << "(p, (size_t)off, v);\n";
-            } else {
-                src << "    p[off] = v;\n";
-            }
-            src << "  }\n};\n";
-            src << "extern \"C\" __global__ void __launch_bounds__(512) " << kname
-                << "(const __grid_constant__ gbfft::fft_params p) {\n"
-                << "  gbfft::fft_tile<" << (q.prec == 4 ? "float" : "double") << ", "
-                << ps.kind << ", gbfft_user_io>(p);\n}\n";
-            mod = nvrtc_build(src.str(), kname, device);
+            std::string src = callback_program(q.cb_source, q.cb_length, q.load_fn, q.store_fn,
+                                               {std::make_tuple(kname, q.prec, ps.kind)});
+            mod = nvrtc_build(src, kname, device);
             if (cache) {
                 cache->store(kname, device, mod);
             }
@@ -1457,6 +1486,68 @@ int bbfft_aot_cache_register_module(bbfft_cache_t cache, const void *image, size
         }
         std::lock_guard<std::mutex> lock(cache->mu);
         cache->aot_modules.push_back(std::move(am));
+    });
+}
+
+int bbfft_aot_generate(const bbfft_configuration *cfgs, size_t num_cfgs, void *image,
+                       size_t image_len, size_t *image_needed, char *names, size_t names_len,
+                       size_t *names_needed) {
+    return guarded([&] {
+        if (!cfgs || num_cfgs == 0) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "no configurations");
+        }
+        const bbfft_configuration &c0 = cfgs[0];
+        std::vector<std::tuple<std::string, int, int>> kernels;
+        std::set<std::string> seen;
+        for (size_t i = 0; i < num_cfgs; ++i) {
+            const bbfft_configuration &c = cfgs[i];
+            gbfft::validate(c);
+            bool has_cb = (c.load_function && *c.load_function) ||
+                          (c.store_function && *c.store_function);
+            if (!has_cb || c.dim != 1) {
+                throw status_error(BBFFT_BAD_CONFIGURATION,
+                                   "only 1d configurations with callbacks need generated "
+                                   "kernels; the others are built into the library");
+            }
+            if (c.callback_length != c0.callback_length ||
+                std::memcmp(c.callback_source, c0.callback_source, c.callback_length) != 0 ||
+                std::strcmp(c.load_function ? c.load_function : "",
+                            c0.load_function ? c0.load_function : "") != 0 ||
+                std::strcmp(c.store_function ? c.store_function : "",
+                            c0.store_function ? c0.store_function : "") != 0) {
+                throw status_error(BBFFT_BAD_CONFIGURATION,
+                                   "all configurations of one image must share the user module");
+            }
+            bool even = c.shape[1] % 2 == 0;
+            int kind = c.type == BBFFT_C2C ? gbfft::kind_c2c
+                       : c.type == BBFFT_R2C
+                           ? (even ? gbfft::kind_r2c_half : gbfft::kind_r2c_full)
+                           : (even ? gbfft::kind_c2r_half : gbfft::kind_c2r_full);
+            std::string name = gbfft::callback_kernel_name(c.precision, kind, c.callback_source,
+                                                           c.callback_length, c.load_function,
+                                                           c.store_function);
+            if (seen.insert(name).second) {
+                kernels.emplace_back(name, c.precision, kind);
+            }
+        }
+        int device = 0;
+        GB_CUDA(cudaGetDevice(&device));
+        std::string src = gbfft::callback_program(c0.callback_source, c0.callback_length,
+                                                  c0.load_function, c0.store_function, kernels);
+        std::vector<char> cubin = gbfft::nvrtc_compile(src, "gbfft_aot", device);
+        if (image_needed) {
+            *image_needed = cubin.size();
+        }
+        if (image && image_len >= cubin.size()) {
+            std::memcpy(image, cubin.data(), cubin.size());
+        } else if (image) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "image buffer too small");
+        }
+        std::string all;
+        for (auto const &k : kernels) {
+            all += std::get<0>(k) + "\n";
+        }
+        copy_string(all, names, names_len, names_needed);
     });
 }
 
