@@ -1,0 +1,2 @@
+// Same declarations as the reference header of this name (see jit_cache.hpp).
+#include "bbfft/jit_cache.hpp"
