@@ -85,6 +85,29 @@ class PlanInfo(ctypes.Structure):
     ]
 
 
+class RaggedItem(ctypes.Structure):
+    _fields_ = [
+        ('precision', ctypes.c_int32),
+        ('direction', ctypes.c_int32),
+        ('type', ctypes.c_int32),
+        ('N', ctypes.c_uint32),
+        ('M', ctypes.c_size_t),
+        ('K', ctypes.c_size_t),
+        ('in_', ctypes.c_void_p),
+        ('out', ctypes.c_void_p),
+    ]
+
+
+class RaggedInfo(ctypes.Structure):
+    _fields_ = [
+        ('num_units', ctypes.c_uint64),
+        ('grid', ctypes.c_uint32),
+        ('block', ctypes.c_uint32),
+        ('shared_bytes', ctypes.c_size_t),
+        ('bytes_moved', ctypes.c_uint64),
+    ]
+
+
 # Every symbol declared in include/bbfft_gb300.h with its ctypes signature.
 _vp = ctypes.c_void_p
 _SIGNATURES = {
@@ -125,6 +148,11 @@ _SIGNATURES = {
     'bbfft_plan_retain': (ctypes.c_int, [_vp]),
     'bbfft_plan_destroy': (ctypes.c_int, [_vp]),
     'bbfft_plan_get_info': (ctypes.c_int, [_vp, ctypes.POINTER(PlanInfo)]),
+    'bbfft_ragged_create': (ctypes.c_int, [ctypes.POINTER(RaggedItem), ctypes.c_size_t,
+                                           ctypes.POINTER(_vp)]),
+    'bbfft_ragged_execute': (ctypes.c_int, [_vp, _vp, ctypes.c_int]),
+    'bbfft_ragged_get_info': (ctypes.c_int, [_vp, ctypes.POINTER(RaggedInfo)]),
+    'bbfft_ragged_destroy': (ctypes.c_int, [_vp]),
     'bbfft_c2r_2d_noalloc_f32': (ctypes.c_int, [_vp, _vp, ctypes.c_size_t, ctypes.c_size_t,
                                                 ctypes.c_size_t, ctypes.c_size_t, _vp]),
     'bbfft_last_error': (ctypes.c_char_p, []),
@@ -314,6 +342,34 @@ class Plan:
 
     def __del__(self):
         self.destroy()
+
+
+class Ragged:
+    """A ragged batch of independent 1d transforms run by one persistent launch.
+
+    items: list of (precision, direction, type, N, M, K, in_ptr, out_ptr) with default
+    packed layouts (include/bbfft_gb300.h: bbfft_ragged_item)."""
+
+    def __init__(self, items):
+        arr = (RaggedItem * len(items))()
+        for i, (prec, d, t, N, M, K, ip, op) in enumerate(items):
+            arr[i] = RaggedItem(prec, d, t, N, M, K, int(ip), int(op))
+        h = _vp()
+        _check(lib().bbfft_ragged_create(arr, len(items), ctypes.byref(h)))
+        self.handle = h
+
+    def execute(self, stream=None, use_graph=False):
+        _check(lib().bbfft_ragged_execute(self.handle, _stream_ptr(stream), int(bool(use_graph))))
+
+    def info(self):
+        i = RaggedInfo()
+        _check(lib().bbfft_ragged_get_info(self.handle, ctypes.byref(i)))
+        return i
+
+    def __del__(self):
+        if getattr(self, 'handle', None) and _lib is not None:
+            _lib.bbfft_ragged_destroy(self.handle)
+            self.handle = None
 
 
 def make_plan(cfg, stream=None, cache=None):

@@ -217,7 +217,7 @@ __device__ __forceinline__ void run_stage(const transform_ctx<R, Kind, IO> &c, i
 #pragma unroll
     for (int it = 0; it < iters; ++it) {
         const int b = j + it * T;
-        if (nb % T != 0 && b >= nb) {
+        if ((NC == 0 || nb % T != 0) && b >= nb) {
             break;
         }
         C v[P];
@@ -363,7 +363,7 @@ __device__ __forceinline__ void r2c_post(const transform_ctx<R, Kind, IO> &c, in
 #pragma unroll
     for (int it = 0; it < iters; ++it) {
         const int i = j + it * T;
-        if (cnt % T != 0 && i >= cnt) {
+        if ((NC == 0 || cnt % T != 0) && i >= cnt) {
             break;
         }
         const int io = Nc - i;
@@ -391,17 +391,23 @@ __device__ __forceinline__ void r2c_post(const transform_ctx<R, Kind, IO> &c, in
 
 template <class R, int Kind, class IO>
 __device__ __forceinline__ transform_ctx<R, Kind, IO> make_ctx(const fft_params &p, void *smem,
-                                                                int T, int Nc, int &j) {
+                                                                int T, int Nc, int &j,
+                                                                long long tile) {
     const int tid = threadIdx.x;
     const int m_l = tid % p.Mb;
     j = (tid / p.Mb) % T;
-    const int k_l = tid / (p.Mb * T);
-    const long long mt = blockIdx.x % p.m_tiles;
-    const long long kt = blockIdx.x / p.m_tiles;
+    int k_l = tid / (p.Mb * T);
+    const long long mt = tile % p.m_tiles;
+    const long long kt = tile / p.m_tiles;
     const long long m = mt * p.Mb + m_l;
     const long long k = kt * p.Kb + k_l;
     transform_ctx<R, Kind, IO> c{p, reinterpret_cast<cplx<R> *>(smem), 0, 0, 0, 0, 0, 0, 0, false};
-    c.active = (m < p.M) && (k < p.K);
+    c.active = (m < p.M) && (k < p.K) && (k_l < p.Kb);
+    if (k_l >= p.Kb) {
+        // thread beyond the tile (persistent CTAs larger than the tile): no butterflies
+        j = 1 << 20;
+        k_l = 0;
+    }
     c.ib = m + k * p.is2;
     c.ob = m + k * p.os2;
     c.sbase = k_l * Nc * p.Mb + m_l;
@@ -413,10 +419,11 @@ __device__ __forceinline__ transform_ctx<R, Kind, IO> make_ctx(const fft_params 
 }
 
 // ---------------------------------------------------------------- runtime-size kernel body
-template <class R, int Kind, class IO> __device__ __forceinline__ void fft_tile(const fft_params &p) {
+template <class R, int Kind, class IO>
+__device__ __forceinline__ void fft_tile_at(const fft_params &p, long long tile) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     int j;
-    auto c = make_ctx<R, Kind, IO>(p, smem_raw, p.T, p.Nc, j);
+    auto c = make_ctx<R, Kind, IO>(p, smem_raw, p.T, p.Nc, j, tile);
     constexpr bool post = Kind == kind_r2c_half;
     int cur = 0;
     int Ns = 1;
@@ -435,6 +442,10 @@ template <class R, int Kind, class IO> __device__ __forceinline__ void fft_tile(
     if constexpr (post) {
         r2c_post<0, 0>(c, j, cur);
     }
+}
+
+template <class R, int Kind, class IO> __device__ __forceinline__ void fft_tile(const fft_params &p) {
+    fft_tile_at<R, Kind, IO>(p, blockIdx.x);
 }
 
 } // namespace gbfft

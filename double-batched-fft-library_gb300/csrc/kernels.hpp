@@ -20,4 +20,7 @@ struct ct_entry {
 };
 const ct_entry *ct_lookup(int prec, int kind, int nc, int T, int V, const int *rad, int L);
 
+// persistent kernel of ragged batches (ragged.cu)
+const void *ragged_kernel_ptr(int prec);
+
 } // namespace gbfft

@@ -391,6 +391,8 @@ struct pass_request {
     int T = 0, Mb = 0, Kb = 0;
     int V = 0; // 0: automatic, 1: no vectorisation along M, > 1: requested width
     bool force_v1 = false;
+    bool runtime_only = false; // runtime-size kernel (ragged batches)
+    int max_block = 0;         // threads per CTA limit (0: kernel default)
 };
 
 // ------------------------------------------------------------------------------------------
@@ -819,7 +821,8 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     long long M = q.M, K = q.K;
     bool has_cb = (q.load_fn && *q.load_fn) || (q.store_fn && *q.store_fn);
     int reqV = q.V, reqMb = q.Mb, reqKb = q.Kb;
-    if (q.radices.empty() && q.T == 0 && q.V == 0 && q.Mb == 0 && q.Kb == 0 && !q.force_v1) {
+    if (q.radices.empty() && q.T == 0 && q.V == 0 && q.Mb == 0 && q.Kb == 0 && !q.force_v1 &&
+        !q.runtime_only) {
         if (auto te = find_tuning(q.prec, ps.kind, N, M)) {
             reqV = te->V;
             reqMb = te->Mb;
@@ -829,7 +832,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     // compile-time-size kernel, vectorised over M when the layout allows it
     const ct_entry *ct = nullptr;
     int V = 1;
-    if (!has_cb) {
+    if (!has_cb && !q.runtime_only) {
         int vw = vector_width(q.prec, rad);
         if (reqV > 0) {
             vw = std::min(vw, reqV);
@@ -844,7 +847,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
             ct = ct_lookup(q.prec, ps.kind, Nc, T, 1, rad.data(), L);
         }
     }
-    int const max_block = ct ? 256 : 512;
+    int const max_block = q.max_block > 0 ? q.max_block : (ct ? 256 : 512);
     // the runtime kernel ping-pongs between two buffers when a stage goes shared->shared;
     // compile-time kernels run their stages in place in one buffer
     int nbuf = 1;
@@ -859,6 +862,9 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     int Mb;
     if (reqMb > 0) {
         Mb = static_cast<int>(std::min<long long>(reqMb, M));
+        if (Mb % V != 0) {
+            Mb = std::max(V, Mb / V * V);
+        }
     } else if (M == 1) {
         Mb = 1;
     } else if (is_real && M <= 64 && (M / V) * T <= max_block) {
@@ -879,7 +885,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         long long last = static_cast<long long>(kb) * Nc * mb - 1;
         return last + (last >> 2) + 1;
     };
-    int Kb = reqKb > 0 ? reqKb : std::max(1, 256 / lanes_per_k);
+    int Kb = reqKb > 0 ? reqKb : std::max(1, std::min(256, max_block) / lanes_per_k);
     Kb = static_cast<int>(std::min<long long>(Kb, K));
     Kb = std::max(Kb, 1);
     while (Kb * lanes_per_k > max_block && Kb > 1) {
@@ -1372,6 +1378,147 @@ static void execute_impl(bbfft_plan_s &plan, const void *in, void *out, cudaStre
 } // namespace gbfft
 
 // ------------------------------------------------------------------------------------------
+// ragged batches
+
+struct bbfft_ragged_s {
+    int device = 0;
+    int prec = 4;
+    std::vector<gbfft::pass> passes; // keep the twiddle tables alive
+    std::unique_ptr<gbfft::device_buffer> items, units, counter;
+    int n_units = 0;
+    unsigned grid = 0, block = 256;
+    std::size_t smem = 0;
+    const void *func = nullptr;
+    uint64_t bytes = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ~bbfft_ragged_s() {
+        if (exec) {
+            cudaGraphExecDestroy(exec);
+        }
+        if (graph) {
+            cudaGraphDestroy(graph);
+        }
+    }
+};
+
+namespace gbfft {
+
+static void make_ragged(bbfft_ragged_item const *items, std::size_t n, bbfft_ragged_s &r) {
+    if (!items || n == 0) {
+        throw status_error(BBFFT_INVALID_ARGUMENT, "empty ragged batch");
+    }
+    r.prec = items[0].precision;
+    for (std::size_t i = 0; i < n; ++i) {
+        auto const &it = items[i];
+        if (it.precision != r.prec) {
+            bad_config("all transforms of a ragged batch share one precision");
+        }
+        if (it.N == 0 || it.M == 0 || it.K == 0) {
+            bad_config("ragged item with an empty shape");
+        }
+        if (!it.in || !it.out) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "ragged item without tensor pointers");
+        }
+        bbfft_configuration c = {};
+        c.dim = 1;
+        c.shape[0] = it.M;
+        c.shape[1] = it.N;
+        c.shape[2] = it.K;
+        c.precision = it.precision;
+        c.type = it.type;
+        c.direction = it.direction;
+        c.istride[0] = c.ostride[0] = 1;
+        validate(c);
+    }
+    GB_CUDA(cudaGetDevice(&r.device));
+    std::vector<ragged_item_dev> dev(n);
+    std::vector<std::pair<double, std::pair<int, int>>> units;
+    int const block = 256;
+    std::size_t smem = 0;
+    for (std::size_t i = 0; i < n; ++i) {
+        auto const &it = items[i];
+        long long N = it.N;
+        long long nin = it.type == BBFFT_C2R ? N / 2 + 1 : N;
+        long long nout = it.type == BBFFT_R2C ? N / 2 + 1 : N;
+        pass_request q{};
+        q.prec = it.precision;
+        q.type = it.type;
+        q.dir = it.direction;
+        q.M = static_cast<long long>(it.M);
+        q.N = N;
+        q.K = static_cast<long long>(it.K);
+        q.is1 = q.M;
+        q.is2 = q.M * nin;
+        q.os1 = q.M;
+        q.os2 = q.M * nout;
+        q.runtime_only = true;
+        q.max_block = block;
+        q.force_v1 = true;
+        r.passes.push_back(make_1d_pass(q, r.device, nullptr));
+        pass const &ps = r.passes.back();
+        dev[i].p = ps.p;
+        dev[i].p.in = it.in;
+        dev[i].p.out = it.out;
+        dev[i].kind = ps.kind;
+        smem = std::max(smem, ps.smem);
+        std::size_t ib = it.type == BBFFT_R2C ? it.precision : 2 * it.precision;
+        std::size_t ob = it.type == BBFFT_C2R ? it.precision : 2 * it.precision;
+        r.bytes += (nin * ib + nout * ob) * it.M * it.K;
+        // cost of one tile ~ elements x (sum of radices): largest first (LPT order)
+        double work = 0;
+        for (int s2 = 0; s2 < ps.p.L; ++s2) {
+            work += ps.p.radix[s2];
+        }
+        double cost = static_cast<double>(ps.p.Mb) * ps.p.Kb * N * (work + 4);
+        for (unsigned t = 0; t < ps.grid; ++t) {
+            units.push_back({cost, {static_cast<int>(i), static_cast<int>(t)}});
+        }
+    }
+    std::stable_sort(units.begin(), units.end(),
+                     [](auto const &a, auto const &b) { return a.first > b.first; });
+    std::vector<int> flat(2 * units.size());
+    for (std::size_t u = 0; u < units.size(); ++u) {
+        flat[2 * u] = units[u].second.first;
+        flat[2 * u + 1] = units[u].second.second;
+    }
+    r.n_units = static_cast<int>(units.size());
+    r.items = std::make_unique<device_buffer>(dev.size() * sizeof(ragged_item_dev));
+    r.units = std::make_unique<device_buffer>(flat.size() * sizeof(int));
+    r.counter = std::make_unique<device_buffer>(sizeof(unsigned));
+    GB_CUDA(cudaMemcpy(r.items->ptr, dev.data(), dev.size() * sizeof(ragged_item_dev),
+                       cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(r.units->ptr, flat.data(), flat.size() * sizeof(int),
+                       cudaMemcpyHostToDevice));
+    r.func = ragged_kernel_ptr(r.prec);
+    r.block = block;
+    r.smem = smem;
+    if (smem > 48 * 1024) {
+        allow_max_smem(r.func, r.device);
+    }
+    int per_sm = 0, sms = 0;
+    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, r.func, block, smem));
+    GB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, r.device));
+    if (per_sm < 1) {
+        bad_config("ragged batch: a unit does not fit on a multiprocessor");
+    }
+    r.grid = static_cast<unsigned>(std::min<long long>(static_cast<long long>(per_sm) * sms,
+                                                       std::max(1, r.n_units)));
+}
+
+static void launch_ragged(bbfft_ragged_s &r, cudaStream_t stream) {
+    GB_CUDA(cudaMemsetAsync(r.counter->ptr, 0, sizeof(unsigned), stream));
+    const void *items = r.items->ptr;
+    const void *units = r.units->ptr;
+    int n = r.n_units;
+    void *counter = r.counter->ptr;
+    void *args[] = {&items, &units, &n, &counter};
+    GB_CUDA(cudaLaunchKernel(r.func, dim3(r.grid), dim3(r.block), args, r.smem, stream));
+}
+
+} // namespace gbfft
+
+// ------------------------------------------------------------------------------------------
 // C ABI
 
 using gbfft::guarded;
@@ -1682,6 +1829,73 @@ int bbfft_plan_destroy(bbfft_plan_t plan) {
             delete plan;
         }
     });
+}
+
+int bbfft_ragged_create(const bbfft_ragged_item *items, size_t num_items, bbfft_ragged_t *ragged) {
+    return guarded([&] {
+        if (!ragged) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "null pointer");
+        }
+        *ragged = nullptr;
+        std::unique_ptr<bbfft_ragged_s> r(new bbfft_ragged_s());
+        gbfft::make_ragged(items, num_items, *r);
+        *ragged = r.release();
+    });
+}
+
+int bbfft_ragged_execute(bbfft_ragged_t ragged, cudaStream_t stream, int use_graph) {
+    return guarded([&] {
+        if (!ragged) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "null ragged batch");
+        }
+        if (!use_graph) {
+            gbfft::launch_ragged(*ragged, stream);
+            return;
+        }
+        if (!ragged->exec) {
+            cudaStream_t cs;
+            GB_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+            cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                try {
+                    gbfft::launch_ragged(*ragged, cs);
+                } catch (...) {
+                    cudaGraph_t g = nullptr;
+                    cudaStreamEndCapture(cs, &g);
+                    if (g) {
+                        cudaGraphDestroy(g);
+                    }
+                    cudaStreamDestroy(cs);
+                    throw;
+                }
+                e = cudaStreamEndCapture(cs, &ragged->graph);
+            }
+            cudaStreamDestroy(cs);
+            if (e != cudaSuccess) {
+                throw status_error(BBFFT_CUDA_ERROR,
+                                   std::string("graph capture failed: ") + cudaGetErrorString(e));
+            }
+            GB_CUDA(cudaGraphInstantiate(&ragged->exec, ragged->graph, 0));
+        }
+        GB_CUDA(cudaGraphLaunch(ragged->exec, stream));
+    });
+}
+
+int bbfft_ragged_get_info(bbfft_ragged_t ragged, bbfft_ragged_info *info) {
+    return guarded([&] {
+        if (!ragged || !info) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "null pointer");
+        }
+        info->num_units = static_cast<uint64_t>(ragged->n_units);
+        info->grid = ragged->grid;
+        info->block = ragged->block;
+        info->shared_bytes = ragged->smem;
+        info->bytes_moved = ragged->bytes;
+    });
+}
+
+int bbfft_ragged_destroy(bbfft_ragged_t ragged) {
+    return guarded([&] { delete ragged; });
 }
 
 int bbfft_plan_get_info(bbfft_plan_t plan, bbfft_plan_info *info) {

@@ -50,3 +50,14 @@ struct fft_params {
 };
 
 } // namespace gbfft
+
+namespace gbfft {
+
+// One transform of a ragged batch: the launch parameters of its pass and the kernel kind.
+struct ragged_item_dev {
+    fft_params p;
+    int kind;
+    int pad_;
+};
+
+} // namespace gbfft

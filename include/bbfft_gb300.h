@@ -206,6 +206,39 @@ BBFFT_GB300_API int bbfft_plan_create_tuned(const bbfft_configuration *cfg, cuda
                                             uint32_t vector_width, uint32_t mb, uint32_t kb,
                                             bbfft_plan_t *plan);
 
+/* ---- ragged batches (no counterpart in the reference, which launches one kernel per plan,
+ *      src/common/algorithm/small_batch_fft.hpp:111) ---- */
+
+/* One independent 1d transform of a ragged batch: default packed layout (c2c: M*N*K
+ * complex in and out; r2c: M*N*K real in, M*(N/2+1)*K complex out; c2r the reverse). */
+typedef struct bbfft_ragged_item {
+    int32_t precision; /* all items of a batch share the precision */
+    int32_t direction;
+    int32_t type;
+    uint32_t N;
+    size_t M, K;
+    const void *in;
+    void *out; /* must not alias another item's input */
+} bbfft_ragged_item;
+typedef struct bbfft_ragged_s *bbfft_ragged_t;
+
+typedef struct bbfft_ragged_info {
+    uint64_t num_units;   /* CTA tiles over all transforms */
+    uint32_t grid, block; /* persistent launch geometry */
+    size_t shared_bytes;  /* dynamic shared memory per CTA */
+    uint64_t bytes_moved; /* algorithmic bytes: one read + one write of every tensor */
+} bbfft_ragged_info;
+
+/* Plans all transforms of the batch for ONE persistent launch on the current device. */
+BBFFT_GB300_API int bbfft_ragged_create(const bbfft_ragged_item *items, size_t num_items,
+                                        bbfft_ragged_t *ragged);
+/* Runs the whole batch: a reset of the work counter and one persistent kernel.  With
+ * use_graph != 0 both are captured once into a CUDA graph that is replayed on `stream`. */
+BBFFT_GB300_API int bbfft_ragged_execute(bbfft_ragged_t ragged, cudaStream_t stream,
+                                         int use_graph);
+BBFFT_GB300_API int bbfft_ragged_get_info(bbfft_ragged_t ragged, bbfft_ragged_info *info);
+BBFFT_GB300_API int bbfft_ragged_destroy(bbfft_ragged_t ragged);
+
 /* Allocation-free 2d c2r, float precision.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory when they transform (during CUDA graph
  * capture, under allocators that forbid cudaMalloc, or with a fixed device footprint).

@@ -1,0 +1,89 @@
+"""Ragged batches: many independent 1d transforms of mixed N, kind and batch sizes in one
+persistent launch (optionally replayed from a CUDA graph), against the FP64 DFT."""
+import numpy as np
+import pytest
+
+from gpu_helpers import TOL, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def make_batch(bb, torch, n, seed, Ns=None):
+    """Seeded batch like the benchmark's: N in {16, 24, ..., 512}, c2c complex64 or r2c
+    float32 50/50, M in {1, 4, 16}, K in [1, 64], data iid U[-1, 1]."""
+    rng = np.random.default_rng(seed)
+    Ns = Ns or list(range(16, 513, 8))
+    specs = []
+    in_off = out_off = 0
+    for _ in range(n):
+        N = int(rng.choice(Ns))
+        t = bb.C2C if rng.random() < 0.5 else bb.R2C
+        M = int(rng.choice([1, 4, 16]))
+        K = int(rng.integers(1, 65))
+        nin = M * N * K * (2 if t == bb.C2C else 1)
+        nout = M * (N if t == bb.C2C else N // 2 + 1) * K * 2
+        specs.append((t, N, M, K, in_off, nin, out_off, nout))
+        in_off += (nin + 3) // 4 * 4      # keep every tensor 16-byte aligned
+        out_off += (nout + 3) // 4 * 4
+    x = torch.empty(in_off, dtype=torch.float32, device='cuda').uniform_(-1, 1)
+    y = torch.zeros(out_off, dtype=torch.float32, device='cuda')
+    items = [(bb.F32, bb.FORWARD, t, N, M, K, x.data_ptr() + 4 * io, y.data_ptr() + 4 * oo)
+             for (t, N, M, K, io, _, oo, _) in specs]
+    return specs, x, y, items
+
+
+def check_items(bb, po, specs, x, y, idx):
+    xh = x.cpu().numpy()
+    yh = y.cpu().numpy()
+    worst = 0.0
+    for i in idx:
+        t, N, M, K, io, nin, oo, nout = specs[i]
+        if t == bb.C2C:
+            xi = xh[io:io + nin].view(np.complex64).reshape(K, N, M)
+        else:
+            xi = xh[io:io + nin].reshape(K, N, M)
+        ref = po.dft64(1, [M, N, K], t, bb.FORWARD, xi)
+        got = yh[oo:oo + nout].view(np.complex64).reshape(ref.shape)
+        e = rel_l2(got, ref)
+        worst = max(worst, e)
+        assert e <= TOL[4], (i, t, N, M, K, e)
+    return worst
+
+
+@pytest.mark.parametrize('use_graph', [False, True])
+def test_ragged_small_batch(bb, po, torch_cuda, use_graph):
+    torch = torch_cuda
+    specs, x, y, items = make_batch(bb, torch, 300, seed=11)
+    r = bb.Ragged(items)
+    info = r.info()
+    assert info.num_units >= len(items) and info.grid >= 1
+    r.execute(torch.cuda.current_stream().cuda_stream, use_graph=use_graph)
+    torch.cuda.synchronize()
+    check_items(bb, po, specs, x, y, range(len(specs)))
+
+
+def test_ragged_benchmark_batch_graph_replay(bb, po, torch_cuda):
+    """The 10^4-transform batch: two graph replays give identical results; a seeded
+    sample of 400 transforms matches the FP64 DFT."""
+    torch = torch_cuda
+    specs, x, y, items = make_batch(bb, torch, 10000, seed=4)
+    r = bb.Ragged(items)
+    s = torch.cuda.current_stream().cuda_stream
+    r.execute(s, use_graph=True)
+    torch.cuda.synchronize()
+    first = y.clone()
+    y.zero_()
+    r.execute(s, use_graph=True)
+    torch.cuda.synchronize()
+    assert torch.equal(first, y)
+    rng = np.random.default_rng(5)
+    check_items(bb, po, specs, x, y, rng.choice(len(specs), 400, replace=False))
+
+
+def test_ragged_rejects_mixed_precision(bb, torch_cuda):
+    torch = torch_cuda
+    a = torch.zeros(1024, device='cuda')
+    items = [(bb.F32, bb.FORWARD, bb.C2C, 16, 1, 1, a.data_ptr(), a.data_ptr() + 512),
+             (bb.F64, bb.FORWARD, bb.C2C, 16, 1, 1, a.data_ptr(), a.data_ptr() + 512)]
+    with pytest.raises(bb.BadConfiguration):
+        bb.Ragged(items)
