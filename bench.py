@@ -297,6 +297,16 @@ def run_ours(args):
 
     # end-to-end through the C ABI with pinned host buffers (rank-local)
     e2e = run_e2e(bb, torch, plans, prec, sptr, stream, args)
+    del xbuf, Xbuf, ybuf
+    torch.cuda.empty_cache()
+    legs = {}
+    if not args.no_legs and rank == 0:
+        legs['c2c_n64_k16384'] = leg_c2c_cfg1(bb, torch, stream, hbm_peak, args.steps, args.warmup)
+        legs['ragged_10k'] = leg_ragged(bb, torch, stream, hbm_peak, args.steps, args.warmup)
+        legs['spectral_layer_2d'] = leg_spectral(bb, torch, stream, args.steps, args.warmup)
+        legs['c2c_3d_64'] = leg_c2c_3d(bb, torch, stream, hbm_peak, args.steps, args.warmup)
+        legs['sweep_f64'] = leg_sweep_f64(bb, torch, stream, hbm_peak, max(2, args.steps // 2), 1)
+        torch.cuda.empty_cache()
 
     line = {
         'metric': METRIC, 'value': round(value, 1), 'unit': 'GB/s', 'n_gpus': ws,
@@ -314,6 +324,7 @@ def run_ours(args):
         'clocks': clk,
         'e2e': e2e,
         'gpu_launches': 2 * len(plans) * args.steps,
+        'legs': legs,
     }
     if rank == 0 and not args.no_cpu:
         line['cpu_baseline'] = cpu_baseline(prec, budget_s=args.cpu_seconds)
@@ -321,6 +332,152 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def event_time(torch, stream, fn, reps):
+    """Average device time of fn() over reps launches (CUDA events on `stream`)."""
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def leg_sweep_f64(bb, torch, stream, hbm_peak, steps, warmup):
+    """Same r2c+c2r sweep in float64 (FP64 arithmetic is the bound on GB300)."""
+    sptr = stream.cuda_stream
+    out = []
+    tot_b, tot_ms = 0, 0.0
+    x = torch.randn((1 << 30) // 8, dtype=torch.float64, device='cuda')
+    maxc = max(M_BATCH * (N // 2 + 1) * k_for(N, 8) for N in SWEEP_N)
+    X = torch.empty(2 * maxc, dtype=torch.float64, device='cuda')
+    y = torch.empty_like(x)
+    for N in SWEEP_N:
+        K = k_for(N, 8)
+        f = bb.Plan(bb.configuration(1, [M_BATCH, N, K], precision=bb.F64, type=bb.R2C), stream=sptr)
+        b = bb.Plan(bb.configuration(1, [M_BATCH, N, K], precision=bb.F64, type=bb.C2R,
+                                     direction=bb.BACKWARD), stream=sptr)
+        for _ in range(warmup):
+            f.execute(x.data_ptr(), X.data_ptr())
+            b.execute(X.data_ptr(), y.data_ptr())
+        tf = event_time(torch, stream, lambda: f.execute(x.data_ptr(), X.data_ptr()), steps)
+        tb = event_time(torch, stream, lambda: b.execute(X.data_ptr(), y.data_ptr()), steps)
+        pb = pass_bytes(N, K, 8)
+        tot_b += 2 * pb
+        tot_ms += tf + tb
+        out.append({'N': N, 'r2c_gbs': round(pb / tf / 1e6, 1), 'c2r_gbs': round(pb / tb / 1e6, 1)})
+    return {'value': round(tot_b / tot_ms / 1e6, 1), 'unit': 'GB/s',
+            'frac_of_hbm': round(tot_b / tot_ms / 1e6 / hbm_peak, 3),
+            'note': 'r2c+c2r M=8, 1 GiB real input per N, float64; FP64-compute-bound on GB300',
+            'per_n': out}
+
+
+def leg_c2c_cfg1(bb, torch, stream, hbm_peak, steps, warmup):
+    """c2c forward complex64, M=1, N=64, K=16384 (8 MiB in + 8 MiB out): 24 rotating
+    input/output pairs (384 MiB) so that consecutive launches miss in L2."""
+    sptr = stream.cuda_stream
+    M, N, K = 1, 64, 16384
+    nb = 24
+    xs = [torch.randn(2 * M * N * K, device='cuda') for _ in range(nb)]
+    ys = [torch.empty(2 * M * N * K, device='cuda') for _ in range(nb)]
+    plan = bb.Plan(bb.configuration(1, [M, N, K], precision=bb.F32), stream=sptr)
+    state = {'i': 0}
+
+    def one():
+        i = state['i'] % nb
+        plan.execute(xs[i].data_ptr(), ys[i].data_ptr())
+        state['i'] += 1
+
+    for _ in range(warmup * nb):
+        one()
+    ms = event_time(torch, stream, one, max(steps, 4) * nb)
+    b = 2 * M * N * K * 8
+    return {'value': round(b / ms / 1e6, 1), 'unit': 'GB/s',
+            'frac_of_hbm': round(b / ms / 1e6 / hbm_peak, 3),
+            'us_per_launch': round(ms * 1e3, 2), 'l2': '24 rotating buffer pairs, 384 MiB'}
+
+
+def ragged_specs(bb, n=10000, seed=4):
+    """The ragged workload: N in {16,...,512} step 8, c2c complex64 / r2c float32 50/50,
+    M in {1,4,16}, K in [1,64]; offsets keep every tensor 16-byte aligned."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    in_off = out_off = 0
+    for _ in range(n):
+        N = int(rng.choice(list(range(16, 513, 8))))
+        t = bb.C2C if rng.random() < 0.5 else bb.R2C
+        M = int(rng.choice([1, 4, 16]))
+        K = int(rng.integers(1, 65))
+        nin = M * N * K * (2 if t == bb.C2C else 1)
+        nout = M * (N if t == bb.C2C else N // 2 + 1) * K * 2
+        specs.append((t, N, M, K, in_off, out_off))
+        in_off += (nin + 3) // 4 * 4
+        out_off += (nout + 3) // 4 * 4
+    return specs, in_off, out_off
+
+
+def leg_ragged(bb, torch, stream, hbm_peak, steps, warmup):
+    """10^4 transforms with U[-1,1] data in one persistent launch replayed from a graph."""
+    specs, nin, nout = ragged_specs(bb)
+    x = torch.empty(nin, dtype=torch.float32, device='cuda').uniform_(-1, 1)
+    y = torch.empty(nout, dtype=torch.float32, device='cuda')
+    items = [(bb.F32, bb.FORWARD, t, N, M, K, x.data_ptr() + 4 * io, y.data_ptr() + 4 * oo)
+             for (t, N, M, K, io, oo) in specs]
+    r = bb.Ragged(items)
+    info = r.info()
+    sptr = stream.cuda_stream
+    for _ in range(warmup):
+        r.execute(sptr, use_graph=True)
+    ms = event_time(torch, stream, lambda: r.execute(sptr, use_graph=True), max(steps, 5))
+    gbs = info.bytes_moved / ms / 1e6
+    return {'value': round(gbs, 1), 'unit': 'GB/s', 'frac_of_hbm': round(gbs / hbm_peak, 3),
+            'ms_per_batch': round(ms, 3), 'bytes_moved': int(info.bytes_moved),
+            'units': int(info.num_units), 'grid': int(info.grid), 'launches_per_batch': 1}
+
+
+def leg_spectral(bb, torch, stream, steps, warmup):
+    """2d r2c 128x128, K = 64 x 32, complex weights on the lowest 32x32 modes, c2r,
+    loss sum(y^2): float32 forward + backward time."""
+    from bbfft_gb300.autograd import SpectralLayer2d
+
+    layer = SpectralLayer2d(128, 128, 64, 32, 32, 32, prec=bb.F32)
+    x = torch.randn(64, 32, 128, 128, device='cuda', requires_grad=True)
+    w = (torch.randn(32, 32, 32, dtype=torch.complex64, device='cuda') * 0.02).requires_grad_(True)
+
+    def step():
+        loss = (layer(x, w) ** 2).sum()
+        loss.backward()
+
+    for _ in range(warmup):
+        step()
+    ms = event_time(torch, stream, step, max(steps, 3))
+    return {'ms_fwd_bwd': round(ms, 3), 'shape': 'r2c/c2r 128x128, K=2048, modes 32x32, f32'}
+
+
+def leg_c2c_3d(bb, torch, stream, hbm_peak, steps, warmup):
+    """3d c2c 64^3 complex64, K=64 (128 MiB), forward and backward (3 passes each)."""
+    sptr = stream.cuda_stream
+    shape = [1, 64, 64, 64, 64]
+    n = 64 ** 4
+    x = torch.randn(2 * n, device='cuda')
+    y = torch.empty_like(x)
+    f = bb.Plan(bb.configuration(3, shape, precision=bb.F32, direction=bb.FORWARD), stream=sptr)
+    b = bb.Plan(bb.configuration(3, shape, precision=bb.F32, direction=bb.BACKWARD), stream=sptr)
+    for _ in range(warmup):
+        f.execute(x.data_ptr(), y.data_ptr())
+        b.execute(y.data_ptr(), x.data_ptr())
+
+    def both():
+        f.execute(x.data_ptr(), y.data_ptr())
+        b.execute(y.data_ptr(), x.data_ptr())
+
+    ms = event_time(torch, stream, both, max(steps, 3))
+    bytes_ = 2 * 3 * 2 * n * 8  # 2 transforms x 3 passes x (read + write)
+    return {'ms_fwd_bwd': round(ms, 3), 'gbs_all_passes': round(bytes_ / ms / 1e6, 1),
+            'frac_of_hbm': round(bytes_ / ms / 1e6 / hbm_peak, 3)}
 
 
 def run_e2e(bb, torch, plans, prec, sptr, stream, args):
@@ -381,6 +538,7 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--cpu-seconds', type=float, default=15.0)
+    ap.add_argument('--no-legs', action='store_true', help='headline workload only')
     args = ap.parse_args()
     if args.impl == 'reference':
         run_reference(args)
