@@ -56,6 +56,7 @@ void clear_fixed_error() { tl_fixed_active = false; }
     do {                                                                                         \
         cudaError_t e_ = (call);                                                                 \
         if (e_ != cudaSuccess) {                                                                 \
+            (void)cudaGetLastError(); /* do not leave a non-sticky error behind */              \
             throw status_error(BBFFT_CUDA_ERROR,                                                 \
                                std::string(#call) + " failed: " + cudaGetErrorString(e_));       \
         }                                                                                        \
@@ -459,8 +460,10 @@ static void allow_max_smem(const void *func, int device) {
     if (done.count({func, device})) {
         return;
     }
+    cudaFuncAttributes attr;
+    GB_CUDA(cudaFuncGetAttributes(&attr, func));
     GB_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 max_optin_smem(device)));
+                                 max_optin_smem(device) - static_cast<int>(attr.sharedSizeBytes)));
     done.insert({func, device});
 }
 
