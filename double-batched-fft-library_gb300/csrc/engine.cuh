@@ -247,8 +247,12 @@ __device__ __forceinline__ void run_stage(const transform_ctx<R, Kind, IO> &c, i
     }
 }
 
-// Radix without an unrolled butterfly: every output is a length-P sum read from shared
-// memory (src must be shared).  O(P) work per output.
+// Odd radix P without an unrolled butterfly (primes above 13).  The stage twiddles are
+// first applied in place to the shared source, then every output pair (k, P-k) is one
+// task: with s_j = x_j + x_{P-j}, d_j = x_j - x_{P-j} (the reference's pair optimisation,
+// src/base/mixed_radix_fft.cpp:55-126)
+//   X_k = x_0 + sum_j cos(2 pi jk/P) s_j - i sum_j sin(2 pi jk/P) d_j,  X_{P-k} likewise,
+// with the w_P table in shared memory.  O(P) work per output.
 template <class R, int Kind, class IO>
 __device__ __forceinline__ void run_stage_generic(const transform_ctx<R, Kind, IO> &c, int j,
                                                   int P, int Ns, int src_buf, bool dst_g,
@@ -256,36 +260,72 @@ __device__ __forceinline__ void run_stage_generic(const transform_ctx<R, Kind, I
     using C = cplx<R>;
     const fft_params &p = c.p;
     const int Nc = p.Nc;
+    const int T = p.T;
     const int nb = Nc / P;
     const C *tw = static_cast<const C *>(p.tw);
-    const int twstride = p.Nt / (Ns * P); // stage twiddle: w_{Ns P}
-    const int wstride = p.Nt / P;         // DFT kernel: w_P
-    for (int idx = j; idx < Nc; idx += p.T) {
-        const int b = idx % nb;
-        const int kf = idx / nb;
-        const int kk = b % Ns;
-        C acc = mk<R>(R(0), R(0));
-        int q = 0; // (jf * kf) mod P
-        for (int jf = 0; jf < P; ++jf) {
-            C x = c.sm[c.sidx(src_buf, b + jf * nb)];
-            if (Ns > 1 && jf > 0) {
-                x = cmul(x, __ldg(tw + jf * kk * twstride));
+    C *wtab = c.sm + p.nbuf * p.buf_elems; // P entries w_P^{-q}
+    const int wstride = p.Nt / P;
+    for (int q = threadIdx.x; q < P; q += blockDim.x) {
+        wtab[q] = __ldg(tw + q * wstride);
+    }
+    if (Ns > 1) {
+        const int twstride = p.Nt / (Ns * P);
+        for (int e = j; e < Nc; e += T) {
+            const int b = e % nb;
+            const int r = e / nb;
+            if (r > 0) {
+                C &v = c.sm[c.sidx(src_buf, e)];
+                v = cmul(v, __ldg(tw + r * (b % Ns) * twstride));
             }
-            C w = __ldg(tw + q * wstride);
-            acc.x += x.x * w.x - x.y * w.y;
-            acc.y += x.x * w.y + x.y * w.x;
-            q += kf;
+        }
+    }
+    __syncthreads();
+    const int H = (P - 1) / 2;
+    for (int task = j; task < nb * (H + 1); task += T) {
+        const int b = task % nb;
+        const int k = task / nb;
+        const int o = b + (b / Ns) * Ns * (P - 1);
+        const C x0 = c.sm[c.sidx(src_buf, b)];
+        if (k == 0) {
+            C sum = x0;
+            for (int jj = 1; jj < P; ++jj) {
+                sum = cadd(sum, c.sm[c.sidx(src_buf, b + jj * nb)]);
+            }
+            if (dst_g) {
+                if (c.active) {
+                    c.template gstore<0>(o, sum);
+                }
+            } else {
+                c.sm[c.sidx(dst_buf, o)] = sum;
+            }
+            continue;
+        }
+        C acc = x0;
+        C bb = mk<R>(R(0), R(0));
+        int q = k;
+        for (int jj = 1; jj <= H; ++jj) {
+            const C xa = c.sm[c.sidx(src_buf, b + jj * nb)];
+            const C xb = c.sm[c.sidx(src_buf, b + (P - jj) * nb)];
+            const C w = wtab[q]; // (cos, -sin)(2 pi q / P)
+            acc.x += w.x * (xa.x + xb.x);
+            acc.y += w.x * (xa.y + xb.y);
+            bb.x += w.y * (xa.x - xb.x);
+            bb.y += w.y * (xa.y - xb.y);
+            q += k;
             if (q >= P) {
                 q -= P;
             }
         }
-        const int o = b + (b / Ns) * Ns * (P - 1) + kf * Ns;
+        const C xk = mk<R>(acc.x - bb.y, acc.y + bb.x);
+        const C xo = mk<R>(acc.x + bb.y, acc.y - bb.x);
         if (dst_g) {
             if (c.active) {
-                c.template gstore<0>(o, acc);
+                c.template gstore<0>(o + k * Ns, xk);
+                c.template gstore<0>(o + (P - k) * Ns, xo);
             }
         } else {
-            c.sm[c.sidx(dst_buf, o)] = acc;
+            c.sm[c.sidx(dst_buf, o + k * Ns)] = xk;
+            c.sm[c.sidx(dst_buf, o + (P - k) * Ns)] = xo;
         }
     }
 }

@@ -794,6 +794,12 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         if (prod != Nc) {
             bad_config("product of radices must equal the complex FFT length " + std::to_string(Nc));
         }
+        for (int r : rad) {
+            if (!unrolled(r) && r % 2 == 0) {
+                bad_config("radix " + std::to_string(r) + " has no butterfly (even radices up to "
+                           "16 only)");
+            }
+        }
     }
     bool post = ps.kind == kind_r2c_half;
     // a generic (non-unrolled) first stage needs a shared-memory source
@@ -883,6 +889,13 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     }
     int const lanes_per_k = (Mb / V) * T;
     std::size_t celem = 2 * static_cast<std::size_t>(q.prec);
+    int pgen = 0; // largest radix without an unrolled butterfly: its w_P table lives in shared
+    for (int r : rad) {
+        if (!unrolled(r)) {
+            pgen = std::max(pgen, r);
+        }
+    }
+    std::size_t const gen_extra = static_cast<std::size_t>(pgen) * celem;
     // shared padding i -> i + (i >> shift) * add adds at most a quarter (choose_padding)
     auto buf_elems = [&](int kb, int mb) {
         long long last = static_cast<long long>(kb) * Nc * mb - 1;
@@ -903,7 +916,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     while (Mb > V && nbuf * buf_elems(Kb, Mb) * celem > soft_limit) {
         Mb = std::max(V, (Mb / 2) / V * V);
     }
-    std::size_t smem = nbuf * buf_elems(Kb, Mb) * celem;
+    std::size_t smem = nbuf * buf_elems(Kb, Mb) * celem + gen_extra;
     if (smem > static_cast<std::size_t>(max_optin_smem(device))) {
         bad_config("FFT length " + std::to_string(N) + " needs " + std::to_string(smem) +
                    " bytes of shared memory per block, more than the device provides");
@@ -935,7 +948,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     p.scale = 1.0;
     // compile-time kernels store lane vectors of 16 bytes or more as swizzled 16-byte planes
     bool planes_kernel = ct != nullptr && celem * V >= 16;
-    smem = static_cast<std::size_t>(nbuf) * choose_layout(p, q.prec, post, V, planes_kernel);
+    smem = static_cast<std::size_t>(nbuf) * choose_layout(p, q.prec, post, V, planes_kernel) + gen_extra;
     // paired real loads / stores: adjacent (unit N-stride, one transform per M) and aligned
     if (ps.kind == kind_r2c_half && q.is1 == 1 && M == 1 && q.is2 % 2 == 0) {
         p.flags |= flag_vec_in;
@@ -1123,7 +1136,13 @@ const char *plan_pass_fixed(int prec, int type, int dir, long long M, long long 
     p.sw_a = 30;
     long long last = static_cast<long long>(Kb) * Nc * Mb - 1;
     p.buf_elems = static_cast<int>(last + (last >> best.sh) * best.ad + 1);
-    smem = static_cast<std::size_t>(nbuf) * p.buf_elems * celem;
+    int pgen = 0;
+    for (int i = 0; i < L; ++i) {
+        if (!unrolled(rad[i])) {
+            pgen = std::max(pgen, rad[i]);
+        }
+    }
+    smem = static_cast<std::size_t>(nbuf) * p.buf_elems * celem + static_cast<std::size_t>(pgen) * celem;
     int optin = 0;
     if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) {
         return "cudaDeviceGetAttribute failed";
@@ -1503,7 +1522,13 @@ static void make_ragged(bbfft_ragged_item const *items, std::size_t n, bbfft_rag
     GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, r.func, block, smem));
     GB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, r.device));
     if (per_sm < 1) {
-        bad_config("ragged batch: a unit does not fit on a multiprocessor");
+        cudaFuncAttributes fa;
+        GB_CUDA(cudaFuncGetAttributes(&fa, r.func));
+        bad_config("ragged batch: a unit does not fit on a multiprocessor (block " +
+                   std::to_string(block) + ", dynamic shared " + std::to_string(smem) +
+                   " B, static " + std::to_string(fa.sharedSizeBytes) + " B, max dynamic " +
+                   std::to_string(fa.maxDynamicSharedSizeBytes) + " B, registers " +
+                   std::to_string(fa.numRegs) + ")");
     }
     r.grid = static_cast<unsigned>(std::min<long long>(static_cast<long long>(per_sm) * sms,
                                                        std::max(1, r.n_units)));
