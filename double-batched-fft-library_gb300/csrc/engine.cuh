@@ -280,52 +280,62 @@ __device__ __forceinline__ void run_stage_generic(const transform_ctx<R, Kind, I
         }
     }
     __syncthreads();
+    // a task computes G output pairs (k, P-k) of one butterfly, so every input pair it
+    // loads serves G outputs; the first task of a butterfly also forms X_0 = x_0 + sum s_j
+    constexpr int G = 4;
     const int H = (P - 1) / 2;
-    for (int task = j; task < nb * (H + 1); task += T) {
+    const int tpb = (H + G - 1) / G; // tasks per butterfly
+    for (int task = j; task < nb * tpb; task += T) {
         const int b = task % nb;
-        const int k = task / nb;
+        const int k0 = 1 + (task / nb) * G;
         const int o = b + (b / Ns) * Ns * (P - 1);
         const C x0 = c.sm[c.sidx(src_buf, b)];
-        if (k == 0) {
-            C sum = x0;
-            for (int jj = 1; jj < P; ++jj) {
-                sum = cadd(sum, c.sm[c.sidx(src_buf, b + jj * nb)]);
-            }
-            if (dst_g) {
-                if (c.active) {
-                    c.template gstore<0>(o, sum);
-                }
-            } else {
-                c.sm[c.sidx(dst_buf, o)] = sum;
-            }
-            continue;
+        C acc[G], bb[G];
+        int q[G];
+        for (int g = 0; g < G; ++g) {
+            acc[g] = x0;
+            bb[g] = mk<R>(R(0), R(0));
+            q[g] = k0 + g;
         }
-        C acc = x0;
-        C bb = mk<R>(R(0), R(0));
-        int q = k;
+        C sum = x0;
         for (int jj = 1; jj <= H; ++jj) {
             const C xa = c.sm[c.sidx(src_buf, b + jj * nb)];
             const C xb = c.sm[c.sidx(src_buf, b + (P - jj) * nb)];
-            const C w = wtab[q]; // (cos, -sin)(2 pi q / P)
-            acc.x += w.x * (xa.x + xb.x);
-            acc.y += w.x * (xa.y + xb.y);
-            bb.x += w.y * (xa.x - xb.x);
-            bb.y += w.y * (xa.y - xb.y);
-            q += k;
-            if (q >= P) {
-                q -= P;
+            const C sj = cadd(xa, xb);
+            const C dj = csub(xa, xb);
+            sum = cadd(sum, sj);
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                const C w = wtab[q[g] < P ? q[g] : 0]; // (cos, -sin)(2 pi q / P)
+                acc[g].x += w.x * sj.x;
+                acc[g].y += w.x * sj.y;
+                bb[g].x += w.y * dj.x;
+                bb[g].y += w.y * dj.y;
+                q[g] += k0 + g;
+                if (q[g] >= P) {
+                    q[g] -= P;
+                }
             }
         }
-        const C xk = mk<R>(acc.x - bb.y, acc.y + bb.x);
-        const C xo = mk<R>(acc.x + bb.y, acc.y - bb.x);
-        if (dst_g) {
-            if (c.active) {
-                c.template gstore<0>(o + k * Ns, xk);
-                c.template gstore<0>(o + (P - k) * Ns, xo);
+        auto put = [&](int kf, C v) {
+            if (dst_g) {
+                if (c.active) {
+                    c.template gstore<0>(o + kf * Ns, v);
+                }
+            } else {
+                c.sm[c.sidx(dst_buf, o + kf * Ns)] = v;
             }
-        } else {
-            c.sm[c.sidx(dst_buf, o + k * Ns)] = xk;
-            c.sm[c.sidx(dst_buf, o + (P - k) * Ns)] = xo;
+        };
+        if (k0 == 1) {
+            put(0, sum);
+        }
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            const int k = k0 + g;
+            if (k <= H) {
+                put(k, mk<R>(acc[g].x - bb[g].y, acc[g].y + bb[g].x));
+                put(P - k, mk<R>(acc[g].x + bb[g].y, acc[g].y - bb[g].x));
+            }
         }
     }
 }
