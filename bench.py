@@ -307,6 +307,8 @@ def run_ours(args):
         legs['c2c_3d_64'] = leg_c2c_3d(bb, torch, stream, hbm_peak, args.steps, args.warmup)
         legs['sweep_f64'] = leg_sweep_f64(bb, torch, stream, hbm_peak, max(2, args.steps // 2), 1)
         torch.cuda.empty_cache()
+        legs['tensor_core_c2c'] = leg_tensor_core(bb, torch, stream, hbm_peak, args.steps, args.warmup)
+        torch.cuda.empty_cache()
 
     line = {
         'metric': METRIC, 'value': round(value, 1), 'unit': 'GB/s', 'n_gpus': ws,
@@ -478,6 +480,40 @@ def leg_c2c_3d(bb, torch, stream, hbm_peak, steps, warmup):
     bytes_ = 2 * 3 * 2 * n * 8  # 2 transforms x 3 passes x (read + write)
     return {'ms_fwd_bwd': round(ms, 3), 'gbs_all_passes': round(bytes_ / ms / 1e6, 1),
             'frac_of_hbm': round(bytes_ / ms / 1e6 / hbm_peak, 3)}
+
+
+def leg_tensor_core(bb, torch, stream, hbm_peak, steps, warmup):
+    """c2c forward, M=1, K=2^20, N in {64, 256, 512}, N(0,1) inputs with a 1e-3 fraction
+    scaled by 1e4: plain FP32 against the tensor-core forms, GB/s and rel-L2 against FP64
+    on a 4096-transform slice."""
+    from oracle import pyoracle as po
+
+    sptr = stream.cuda_stream
+    K = 1 << 20
+    out = {}
+    for N in (64, 256, 512):
+        g = torch.Generator(device='cuda')
+        g.manual_seed(N)
+        x = torch.randn(2 * N * K, device='cuda', generator=g)
+        sel = torch.rand(2 * N * K, device='cuda', generator=g) < 1e-3
+        x[sel] *= 1e4
+        y = torch.empty_like(x)
+        xs = x[:2 * N * 4096].cpu().numpy().view(np.complex64).astype(np.complex128)
+        ref = po.dft64(1, [1, N, 4096], po.C2C, po.FORWARD, xs.reshape(4096, N, 1))
+        row = {}
+        for name, mode in (('fp32', 0), ('bf16', 1), ('split_bf16_3term', 3), ('split_bf16_6term', 2)):
+            plan = bb.Plan(bb.configuration(1, [1, N, K], precision=bb.F32, compute=mode), stream=sptr)
+            for _ in range(warmup):
+                plan.execute(x.data_ptr(), y.data_ptr())
+            ms = event_time(torch, stream, lambda: plan.execute(x.data_ptr(), y.data_ptr()), max(steps, 3))
+            got = y[:2 * N * 4096].cpu().numpy().view(np.complex64).reshape(ref.shape)
+            err = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+            gbs = 2 * N * K * 8 / ms / 1e6
+            row[name] = {'gbs': round(gbs, 1), 'frac_of_hbm': round(gbs / hbm_peak, 3),
+                         'rel_l2': float('%.3g' % err)}
+        out['N%d' % N] = row
+        del x, y
+    return out
 
 
 def run_e2e(bb, torch, plans, prec, sptr, stream, args):

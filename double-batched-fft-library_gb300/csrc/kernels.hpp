@@ -1,6 +1,8 @@
 // Host-visible handles of the AOT-compiled kernels.
 #pragma once
 
+#include <cstddef>
+
 namespace gbfft {
 
 // runtime-size kernels, one per transform kind
@@ -19,6 +21,11 @@ struct ct_entry {
     const void *fn;
 };
 const ct_entry *ct_lookup(int prec, int kind, int nc, int T, int V, const int *rad, int L);
+
+// tensor-core DFT stages (tc.cu)
+const void *tc_kernel(int pieces, int nc);
+std::size_t tc_shared_bytes();
+int tc_tile_transforms(int nc);
 
 // persistent kernel of ragged batches (ragged.cu)
 const void *ragged_kernel_ptr(int prec);

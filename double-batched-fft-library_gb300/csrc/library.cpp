@@ -371,6 +371,7 @@ struct pass {
     std::shared_ptr<device_buffer> tw;
     bool inplace_ok = true;
     bool specialized = false; // compile-time-size kernel
+    bool tc = false;          // tensor-core DFT stages
     int V = 1;                // transforms per thread along M
     std::shared_ptr<pass> scalar_alt; // V = 1 variant for pointers not aligned to 16 bytes
     std::string identifier;
@@ -393,6 +394,7 @@ struct pass_request {
     int V = 0; // 0: automatic, 1: no vectorisation along M, > 1: requested width
     bool force_v1 = false;
     bool runtime_only = false; // runtime-size kernel (ragged batches)
+    int compute = BBFFT_COMPUTE_NATIVE;
     int max_block = 0;         // threads per CTA limit (0: kernel default)
 };
 
@@ -802,6 +804,34 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         }
     }
     bool post = ps.kind == kind_r2c_half;
+    if (q.compute != BBFFT_COMPUTE_NATIVE) {
+        // tensor-core DFT stages (tc.cu): fixed tiles of whole transforms
+        int pieces = q.compute == BBFFT_COMPUTE_BF16 ? 1 : q.compute == BBFFT_COMPUTE_SPLIT_BF16_3TERM ? 2 : 3;
+        fft_params &p = ps.p;
+        p.M = 1;
+        p.K = q.K;
+        p.is1 = p.os1 = 1;
+        p.is2 = q.is2;
+        p.os2 = q.os2;
+        p.N = p.Nc = p.Nt = N;
+        p.flags = flags;
+        p.scale = 1.0;
+        int tiles = tc_tile_transforms(N);
+        ps.grid = static_cast<unsigned>((q.K + tiles - 1) / tiles);
+        ps.block = 256;
+        ps.smem = tc_shared_bytes();
+        ps.func = tc_kernel(pieces, N);
+        ps.tc = true;
+        ps.inplace_ok = true;
+        ps.tw = get_twiddles(device, q.prec, N);
+        p.tw = ps.tw->ptr;
+        ps.identifier = "gbfft_tc_p" + std::to_string(pieces) + "_N" + std::to_string(N) + "_K" +
+                        std::to_string(q.K);
+        if (!ps.func) {
+            throw status_error(BBFFT_INTERNAL_ERROR, "tensor-core kernel not found");
+        }
+        return ps;
+    }
     // a generic (non-unrolled) first stage needs a shared-memory source
     if (!unrolled(rad.front())) {
         rad.insert(rad.begin(), 1);
@@ -1207,7 +1237,18 @@ static void validate(bbfft_configuration const &cfg) {
         bad_config("stride s0 != 1 is not supported");
     }
     if (cfg.compute != BBFFT_COMPUTE_NATIVE) {
-        bad_config("compute mode not available for this configuration");
+        bool ok = cfg.compute == BBFFT_COMPUTE_BF16 || cfg.compute == BBFFT_COMPUTE_SPLIT_BF16 ||
+                  cfg.compute == BBFFT_COMPUTE_SPLIT_BF16_3TERM;
+        std::size_t N = cfg.shape[1];
+        ok = ok && cfg.dim == 1 && cfg.type == BBFFT_C2C && cfg.precision == BBFFT_PRECISION_F32 &&
+             (N == 64 || N == 256 || N == 512) && cfg.shape[0] == 1 && cfg.istride[1] == 1 &&
+             cfg.ostride[1] == 1 && cfg.istride[2] == N && cfg.ostride[2] == N &&
+             !(cfg.load_function && *cfg.load_function) &&
+             !(cfg.store_function && *cfg.store_function);
+        if (!ok) {
+            bad_config("tensor-core compute modes support 1d c2c float transforms of length 64, "
+                       "256 or 512 with M = 1 and the packed layout, without callbacks");
+        }
     }
 }
 
@@ -1265,6 +1306,7 @@ static void make_plan_impl(bbfft_configuration const &cfg, cudaStream_t stream,
         q.cb_length = cfg.callback_length;
         q.load_fn = cfg.load_function;
         q.store_fn = cfg.store_function;
+        q.compute = adjoint ? BBFFT_COMPUTE_NATIVE : cfg.compute;
         plan.passes.push_back(make_1d_pass(q, plan.device, cache));
         plan.inplace_ok = plan.passes.back().inplace_ok;
         plan.jit = has_cb;
@@ -1367,10 +1409,13 @@ static void execute_impl(bbfft_plan_s &plan, const void *in, void *out, cudaStre
     for (auto &pass0 : plan.passes) {
         const void *pin = pass0.in_sel == 0 ? in : tmp;
         void *pout = pass0.out_sel == 1 ? out : tmp;
-        pass const &ps = (pass0.V > 1 && ((reinterpret_cast<std::uintptr_t>(pin) |
-                                           reinterpret_cast<std::uintptr_t>(pout)) % 16))
-                             ? *pass0.scalar_alt
-                             : pass0;
+        bool misaligned = ((reinterpret_cast<std::uintptr_t>(pin) |
+                            reinterpret_cast<std::uintptr_t>(pout)) % 16) != 0;
+        if (pass0.tc && misaligned) {
+            throw status_error(BBFFT_INVALID_ARGUMENT,
+                               "tensor-core plans need 16-byte aligned tensors");
+        }
+        pass const &ps = (pass0.V > 1 && misaligned) ? *pass0.scalar_alt : pass0;
         fft_params p = ps.p;
         p.in = pin;
         p.out = pout;

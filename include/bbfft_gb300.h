@@ -65,9 +65,12 @@ typedef enum bbfft_status {
 
 /* Arithmetic used by the DFT stages (no counterpart in the reference, which computes in
  * the plan precision only).  F32 plans only; F64 plans always use BBFFT_COMPUTE_NATIVE. */
-#define BBFFT_COMPUTE_NATIVE 0    /* plain FP32 / FP64 on CUDA cores */
-#define BBFFT_COMPUTE_BF16 1      /* tensor-core DFT stages, BF16 operands, FP32 accumulate */
-#define BBFFT_COMPUTE_SPLIT_BF16 2 /* tensor-core DFT stages, 3-term split-BF16 products */
+#define BBFFT_COMPUTE_NATIVE 0     /* plain FP32 / FP64 on CUDA cores */
+#define BBFFT_COMPUTE_BF16 1       /* tensor-core radix-16 stages, BF16 operands, FP32 accumulate */
+#define BBFFT_COMPUTE_SPLIT_BF16 2 /* operands split in 3 BF16 pieces, 6 product terms (~FP32) */
+#define BBFFT_COMPUTE_SPLIT_BF16_3TERM 3 /* operands split in 2 BF16 pieces, 3 product terms */
+/* The tensor-core modes apply to 1d c2c float plans with N in {64, 256, 512}, M = 1 and the
+ * packed layout; other configurations reject them with BBFFT_BAD_CONFIGURATION. */
 
 /*
  * FFT configuration; mirrors bbfft::configuration (reference
