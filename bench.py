@@ -566,6 +566,36 @@ def run_e2e(bb, torch, plans, prec, sptr, stream, args):
                         'buffers, copies inside the timed region'}
 
 
+def run_profile(args):
+    """Launches for an ncu capture, no timing: `step` runs every plan of one benchmark step
+    once (28 launches); `case` runs one plan once (KIND:N, KIND in r2c / c2r, float32,
+    M=8, 1 GiB real input -- or c2c:N with M=1, K=2^20)."""
+    import torch
+
+    import bbfft_gb300 as bb
+
+    stream = torch.cuda.current_stream().cuda_stream
+    if args.profile == 'step':
+        cases = [(t, N) for N in SWEEP_N for t in ('r2c', 'c2r')]
+    else:
+        kind, n = args.profile_case.split(':')
+        cases = [(kind, int(n))]
+    x = torch.randn((1 << 30) // 4 + 64, device='cuda')
+    y = torch.empty(300 << 20, device='cuda')
+    for kind, N in cases:
+        if kind == 'c2c':
+            cfg = bb.configuration(1, [1, N, 1 << 20], precision=bb.F32)
+        elif kind == 'r2c':
+            cfg = bb.configuration(1, [M_BATCH, N, k_for(N, 4)], precision=bb.F32, type=bb.R2C)
+        else:
+            cfg = bb.configuration(1, [M_BATCH, N, k_for(N, 4)], precision=bb.F32, type=bb.C2R,
+                                   direction=bb.BACKWARD)
+        plan = bb.Plan(cfg, stream=stream)
+        plan.execute(x.data_ptr(), y.data_ptr())
+    torch.cuda.synchronize()
+    print('profiled launches:', len(cases))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -575,7 +605,12 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--cpu-seconds', type=float, default=15.0)
     ap.add_argument('--no-legs', action='store_true', help='headline workload only')
+    ap.add_argument('--profile', choices=['step', 'case'], help='launches for an ncu capture')
+    ap.add_argument('--profile-case', default='c2r:160')
     args = ap.parse_args()
+    if args.profile:
+        run_profile(args)
+        return
     if args.impl == 'reference':
         run_reference(args)
     else:
