@@ -320,7 +320,8 @@ def run_ours(args):
                    'parallelism': 'K-slab per rank, no collectives' if ws > 1 else 'single GPU'},
         'roofline': {'bound': 'hbm', 'achieved': round(achieved, 1), 'peak': hbm_peak,
                      'unit': 'GB/s', 'frac': round(achieved / hbm_peak, 4), 'traffic': traffic,
-                     'peak_kind': peak_kind, 'kernel': 'gbfft::fft_kernel<float, kind> (all '
+                     'algorithmic_bytes': total_bytes, 'per': 'step (28 launches)',
+                     'peak_kind': peak_kind, 'kernel': 'fft_kernel_ct<float, kind, ...> (all '
                      'launches of the step; algorithmic bytes = one read + one write)'},
         'per_n': per_n,
         'clocks': clk,
@@ -580,16 +581,28 @@ def run_profile(args):
     else:
         kind, n = args.profile_case.split(':')
         cases = [(kind, int(n))]
-    x = torch.randn((1 << 30) // 4 + 64, device='cuda')
-    y = torch.empty(300 << 20, device='cuda')
+    cfgs = []
     for kind, N in cases:
         if kind == 'c2c':
             cfg = bb.configuration(1, [1, N, 1 << 20], precision=bb.F32)
+            nin = nout = 2 * N * (1 << 20)
         elif kind == 'r2c':
-            cfg = bb.configuration(1, [M_BATCH, N, k_for(N, 4)], precision=bb.F32, type=bb.R2C)
-        else:
-            cfg = bb.configuration(1, [M_BATCH, N, k_for(N, 4)], precision=bb.F32, type=bb.C2R,
+            K = k_for(N, 4)
+            cfg = bb.configuration(1, [M_BATCH, N, K], precision=bb.F32, type=bb.R2C)
+            nin, nout = M_BATCH * N * K, 2 * M_BATCH * (N // 2 + 1) * K
+        elif kind == 'c2r':
+            K = k_for(N, 4)
+            cfg = bb.configuration(1, [M_BATCH, N, K], precision=bb.F32, type=bb.C2R,
                                    direction=bb.BACKWARD)
+            nin, nout = 2 * M_BATCH * (N // 2 + 1) * K, M_BATCH * N * K
+        else:
+            raise SystemExit('unknown profile case ' + kind)
+        cfgs.append((cfg, nin, nout))
+    # buffers sized from the largest input / output extent (in floats) of the cases
+    x = torch.randn(max(c[1] for c in cfgs), device='cuda')
+    y = torch.empty(max(c[2] for c in cfgs), device='cuda')
+    for cfg, nin, nout in cfgs:
+        assert nin <= x.numel() and nout <= y.numel()
         plan = bb.Plan(cfg, stream=stream)
         plan.execute(x.data_ptr(), y.data_ptr())
     torch.cuda.synchronize()

@@ -386,5 +386,34 @@ def c2r_2d_noalloc_f32(inp, out, M, N1, N2, K, stream=None):
     _check(lib().bbfft_c2r_2d_noalloc_f32(int(inp), int(out), M, N1, N2, K, _stream_ptr(stream)))
 
 
+def shard_k(cfg, world, rank):
+    """K slab of one rank when a transform is split over `world` GPUs.
+
+    Every (m, k) transform of the tensor is independent, so the tensor is cut along K
+    (shape[dim + 1]) into `world` contiguous slabs, one per rank, with no exchange between
+    ranks.  Returns (k0, k1, in_offset, out_offset, slab): the rank's K range, the byte
+    offsets of its first input and output element (k0 * stride[dim + 1] elements), and a
+    configuration of the slab with the caller's strides (None when the rank gets no
+    transform).  Plans of the slab run on the rank's own GPU on `in + in_offset`,
+    `out + out_offset`."""
+    dim = cfg.dim
+    K = int(cfg.shape[dim + 1])
+    k0 = rank * K // world
+    k1 = (rank + 1) * K // world
+    real = 4 if cfg.precision == F32 else 8
+    isz = real if cfg.type == R2C else 2 * real
+    osz = real if cfg.type == C2R else 2 * real
+    in_off = k0 * int(cfg.istride[dim + 1]) * isz
+    out_off = k0 * int(cfg.ostride[dim + 1]) * osz
+    if k1 == k0:
+        return k0, k1, in_off, out_off, None
+    slab = Configuration()
+    ctypes.memmove(ctypes.byref(slab), ctypes.byref(cfg), ctypes.sizeof(Configuration))
+    if hasattr(cfg, '_keep'):
+        slab._keep = cfg._keep
+    slab.shape[dim + 1] = k1 - k0
+    return k0, k1, in_off, out_off, slab
+
+
 def version():
     return lib().bbfft_version().decode()

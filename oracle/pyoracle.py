@@ -4,8 +4,8 @@ Two independent references:
   * `oracle_fft`: the C restatement of the reference's algorithm (bbfft_oracle.c),
     in the plan precision or FP64, with the reference's nd chaining
     (src/common/algorithm/nd_fft.hpp:27-176);
-  * `dft64`: an FP64 DFT (numpy pocketfft in float64, and a naive O(N^2)
-    long-double DFT for small N) used to measure rel-L2 errors.
+  * `dft64`: an FP64 DFT (numpy pocketfft in float64) with the reference's c2r
+    semantics, used to measure rel-L2 errors.
 Plus the analytic known-answer signals of the reference's device tests
 (test/c2c.cpp:17-51, test/r2c.cpp:28-135), reimplemented.
 

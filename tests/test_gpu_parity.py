@@ -257,3 +257,42 @@ def test_random_vs_oracle(bb, po, torch_cuda, prec, type):
             worst = max(worst, e)
             assert e <= TOL[prec], (N, M, K, direction, e)
     print('worst rel-L2', worst)
+
+
+# ------------------------------------------------- full benchmark sizes (1 GiB per pass)
+
+SWEEP_N = [16, 32, 64, 128, 256, 512, 48, 96, 160, 224, 384, 7, 11, 13]
+
+
+@pytest.mark.parametrize('N', SWEEP_N)
+def test_full_size_round_trip(bb, po, torch_cuda, N):
+    """At the benchmark's full size (float, M=8, K = 2^30 / (4 * 8 * N), 1 GiB real input):
+    c2r(r2c(x)) = N x to rel-L2 <= 2e-6, and 24 sampled k-slices of the r2c output equal
+    the FP64 transform of those slices (rel-L2 <= 2e-6) and the oracle."""
+    torch = torch_cuda
+    M, K = 8, (1 << 30) // (4 * 8 * N)
+    nc = N // 2 + 1
+    stream = torch.cuda.current_stream().cuda_stream
+    g = torch.Generator(device='cuda')
+    g.manual_seed(N)
+    x = torch.randn(M * N * K, device='cuda', generator=g)
+    X = torch.empty(2 * M * nc * K, device='cuda')
+    y = torch.empty(M * N * K, device='cuda')
+    fwd = bb.Plan(bb.configuration(1, [M, N, K], precision=bb.F32, type=bb.R2C), stream=stream)
+    bwd = bb.Plan(bb.configuration(1, [M, N, K], precision=bb.F32, type=bb.C2R,
+                                   direction=bb.BACKWARD), stream=stream)
+    fwd.execute(x.data_ptr(), X.data_ptr())
+    bwd.execute(X.data_ptr(), y.data_ptr())
+    torch.cuda.synchronize()
+    err = float(torch.linalg.vector_norm(y / N - x) / torch.linalg.vector_norm(x))
+    assert err <= 2e-6, err
+    ks = np.random.default_rng(N).choice(K, 24, replace=False)
+    ks = torch.tensor(np.sort(ks), device='cuda')
+    xs = x.view(K, N * M)[ks].cpu().numpy()
+    Xs = torch.view_as_complex(X.view(K, nc * M, 2)[ks]).cpu().numpy()
+    ref = po.dft64(1, [M, N, 24], po.R2C, po.FORWARD, xs.reshape(24, N, M))
+    assert rel_l2(Xs.reshape(ref.shape), ref) <= 2e-6
+    orc = po.oracle_fft(1, [M, N, 24], po.R2C, po.FORWARD, xs.ravel(), prec=4)
+    assert rel_l2(Xs.ravel(), orc) <= 2e-6
+    del x, X, y
+    torch.cuda.empty_cache()
