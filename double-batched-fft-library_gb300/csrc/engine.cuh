@@ -248,11 +248,21 @@ __device__ __forceinline__ void run_stage(const transform_ctx<R, Kind, IO> &c, i
 }
 
 // Odd radix P without an unrolled butterfly (primes above 13).  The stage twiddles are
-// first applied in place to the shared source, then every output pair (k, P-k) is one
-// task: with s_j = x_j + x_{P-j}, d_j = x_j - x_{P-j} (the reference's pair optimisation,
-// src/base/mixed_radix_fft.cpp:55-126)
-//   X_k = x_0 + sum_j cos(2 pi jk/P) s_j - i sum_j sin(2 pi jk/P) d_j,  X_{P-k} likewise,
-// with the w_P table in shared memory.  O(P) work per output.
+// first applied in place to the shared source; then every output pair (k, P-k) comes
+// from the pair sums s_j = x_j + x_{P-j}, d_j = x_j - x_{P-j} (the reference's pair
+// optimisation, src/base/mixed_radix_fft.cpp:55-126):
+//   X_k = x_0 + sum_j cos(2 pi jk/P) s_j - i sum_j sin(2 pi jk/P) d_j,  X_{P-k} likewise.
+// O(P) work per output.
+//
+// P <= gen_table_max_p: a thread computes whole butterflies, G output pairs per sweep over
+// the input pairs, and the coefficients come from a k-major table w_P^{-(jk mod P)} in
+// shared memory (rows padded to a multiple of G with zeros).  Every lane of a warp reads
+// the same coefficient at the same time (one broadcast load per four FMAs).
+// Larger P: tasks of G output pairs over the threads, coefficients from the w_P table.
+__device__ __forceinline__ int gen_table_rows(int P) {
+    return ((P - 1) / 2 + gen_group - 1) / gen_group * gen_group;
+}
+
 template <class R, int Kind, class IO>
 __device__ __forceinline__ void run_stage_generic(const transform_ctx<R, Kind, IO> &c, int j,
                                                   int P, int Ns, int src_buf, bool dst_g,
@@ -263,10 +273,22 @@ __device__ __forceinline__ void run_stage_generic(const transform_ctx<R, Kind, I
     const int T = p.T;
     const int nb = Nc / P;
     const C *tw = static_cast<const C *>(p.tw);
-    C *wtab = c.sm + p.nbuf * p.buf_elems; // P entries w_P^{-q}
+    C *wtab = c.sm + p.nbuf * p.buf_elems;
     const int wstride = p.Nt / P;
-    for (int q = threadIdx.x; q < P; q += blockDim.x) {
-        wtab[q] = __ldg(tw + q * wstride);
+    const int H = (P - 1) / 2;
+    const bool table = P <= gen_table_max_p;
+    if (table) {
+        // wtab[(k - 1) * H + (jj - 1)] = w_P^{-(jj k mod P)}, k = 1 .. rows
+        const int rows = gen_table_rows(P);
+        for (int e = threadIdx.x; e < rows * H; e += blockDim.x) {
+            const int k = e / H + 1;
+            const int jj = e % H + 1;
+            wtab[e] = k <= H ? __ldg(tw + ((jj * k) % P) * wstride) : mk<R>(R(0), R(0));
+        }
+    } else {
+        for (int q = threadIdx.x; q < P; q += blockDim.x) {
+            wtab[q] = __ldg(tw + q * wstride);
+        }
     }
     if (Ns > 1) {
         const int twstride = p.Nt / (Ns * P);
@@ -280,10 +302,62 @@ __device__ __forceinline__ void run_stage_generic(const transform_ctx<R, Kind, I
         }
     }
     __syncthreads();
+    auto put = [&](int o, int kf, C v) {
+        if (dst_g) {
+            if (c.active) {
+                c.template gstore<0>(o + kf * Ns, v);
+            }
+        } else {
+            c.sm[c.sidx(dst_buf, o + kf * Ns)] = v;
+        }
+    };
+    constexpr int G = gen_group;
+    if (table) {
+        for (int b = j; b < nb; b += T) {
+            const int o = b + (b / Ns) * Ns * (P - 1);
+            const C x0 = c.sm[c.sidx(src_buf, b)];
+            for (int k0 = 1; k0 <= H; k0 += G) {
+                const C *w = wtab + (k0 - 1) * H;
+                C acc[G], dd[G];
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    acc[g] = x0;
+                    dd[g] = mk<R>(R(0), R(0));
+                }
+                C sum = x0;
+#pragma unroll 2
+                for (int jj = 1; jj <= H; ++jj) {
+                    const C xa = c.sm[c.sidx(src_buf, b + jj * nb)];
+                    const C xb = c.sm[c.sidx(src_buf, b + (P - jj) * nb)];
+                    const C sj = cadd(xa, xb);
+                    const C dj = csub(xa, xb);
+                    sum = cadd(sum, sj);
+#pragma unroll
+                    for (int g = 0; g < G; ++g) {
+                        const C cw = w[g * H + jj - 1]; // (cos, -sin)(2 pi jj k / P)
+                        acc[g].x += cw.x * sj.x;
+                        acc[g].y += cw.x * sj.y;
+                        dd[g].x += cw.y * dj.x;
+                        dd[g].y += cw.y * dj.y;
+                    }
+                }
+                if (k0 == 1) {
+                    put(o, 0, sum);
+                }
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    const int k = k0 + g;
+                    if (k <= H) {
+                        put(o, k, mk<R>(acc[g].x - dd[g].y, acc[g].y + dd[g].x));
+                        put(o, P - k, mk<R>(acc[g].x + dd[g].y, acc[g].y - dd[g].x));
+                    }
+                }
+            }
+        }
+        return;
+    }
     // a task computes G output pairs (k, P-k) of one butterfly, so every input pair it
     // loads serves G outputs; the first task of a butterfly also forms X_0 = x_0 + sum s_j
-    constexpr int G = 4;
-    const int H = (P - 1) / 2;
     const int tpb = (H + G - 1) / G; // tasks per butterfly
     for (int task = j; task < nb * tpb; task += T) {
         const int b = task % nb;
@@ -317,24 +391,15 @@ __device__ __forceinline__ void run_stage_generic(const transform_ctx<R, Kind, I
                 }
             }
         }
-        auto put = [&](int kf, C v) {
-            if (dst_g) {
-                if (c.active) {
-                    c.template gstore<0>(o + kf * Ns, v);
-                }
-            } else {
-                c.sm[c.sidx(dst_buf, o + kf * Ns)] = v;
-            }
-        };
         if (k0 == 1) {
-            put(0, sum);
+            put(o, 0, sum);
         }
 #pragma unroll
         for (int g = 0; g < G; ++g) {
             const int k = k0 + g;
             if (k <= H) {
-                put(k, mk<R>(acc[g].x - bb[g].y, acc[g].y + bb[g].x));
-                put(P - k, mk<R>(acc[g].x + bb[g].y, acc[g].y - bb[g].x));
+                put(o, k, mk<R>(acc[g].x - bb[g].y, acc[g].y + bb[g].x));
+                put(o, P - k, mk<R>(acc[g].x + bb[g].y, acc[g].y - bb[g].x));
             }
         }
     }

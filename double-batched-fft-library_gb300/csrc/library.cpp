@@ -284,6 +284,20 @@ std::vector<char> nvrtc_compile(std::string const &source, std::string const &na
 // algorithm selection and blocking
 
 static bool unrolled(int P) { return P == 1 || (P >= 2 && P <= 13) || P == 16; }
+// Generic (non-unrolled) odd radix with the coefficient table of run_stage_generic
+// (engine.cuh): one thread per butterfly.
+static bool table_generic(int P) { return !unrolled(P) && P % 2 == 1 && P <= gen_table_max_p; }
+// shared-memory elements the generic stage of radix P needs after the data buffers
+static int gen_shared_elems(int P) {
+    if (unrolled(P)) {
+        return 0;
+    }
+    if (P <= gen_table_max_p) {
+        int H = (P - 1) / 2;
+        return (H + gen_group - 1) / gen_group * gen_group * H;
+    }
+    return P;
+}
 
 // Radices for an Nc-point complex FFT: few stages, unrolled butterflies where possible.
 // Writes at most 32 radices to `out` and returns their number (no allocation).
@@ -855,6 +869,16 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     if (pu == 1) {
         T = std::min(Nc, 64);
     }
+    // with a table-driven generic stage: one thread per butterfly of the largest one
+    int ptg = 0;
+    for (int r : rad) {
+        if (table_generic(r)) {
+            ptg = std::max(ptg, r);
+        }
+    }
+    if (ptg > 0 && q.T <= 0) {
+        T = Nc / ptg;
+    }
     T = std::min(T, 512);
 
     long long M = q.M, K = q.K;
@@ -919,11 +943,9 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     }
     int const lanes_per_k = (Mb / V) * T;
     std::size_t celem = 2 * static_cast<std::size_t>(q.prec);
-    int pgen = 0; // largest radix without an unrolled butterfly: its w_P table lives in shared
+    int pgen = 0; // generic stages keep their coefficient tables in shared memory
     for (int r : rad) {
-        if (!unrolled(r)) {
-            pgen = std::max(pgen, r);
-        }
+        pgen = std::max(pgen, gen_shared_elems(r));
     }
     std::size_t const gen_extra = static_cast<std::size_t>(pgen) * celem;
     // shared padding i -> i + (i >> shift) * add adds at most a quarter (choose_padding)
@@ -1168,9 +1190,7 @@ const char *plan_pass_fixed(int prec, int type, int dir, long long M, long long 
     p.buf_elems = static_cast<int>(last + (last >> best.sh) * best.ad + 1);
     int pgen = 0;
     for (int i = 0; i < L; ++i) {
-        if (!unrolled(rad[i])) {
-            pgen = std::max(pgen, rad[i]);
-        }
+        pgen = std::max(pgen, gen_shared_elems(rad[i]));
     }
     smem = static_cast<std::size_t>(nbuf) * p.buf_elems * celem + static_cast<std::size_t>(pgen) * celem;
     int optin = 0;

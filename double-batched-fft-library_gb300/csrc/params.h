@@ -6,6 +6,11 @@ namespace gbfft {
 
 constexpr int max_stages = 12;
 
+// generic odd radices up to gen_table_max_p use a shared k-major coefficient table with
+// rows padded to a multiple of gen_group (output pairs per sweep)
+constexpr int gen_table_max_p = 61;
+constexpr int gen_group = 8;
+
 enum kind : int {
     kind_c2c = 0,
     kind_r2c_half = 1, // even N: N/2-point complex FFT + post-process

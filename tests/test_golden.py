@@ -81,17 +81,18 @@ def test_cuda_known_answer_vectors(bb, po, torch_cuda):
 
     z = np.load(os.path.join(HERE, 'known_answers.npz'))
     for prec in (4, 8):
+        rdt, cdt = (np.float32, np.complex64) if prec == 4 else (np.float64, np.complex128)
         for N in (8, 13, 64):
             x, X = z[f'c2c_{prec}_{N}_x'], z[f'c2c_{prec}_{N}_X']
             cfg = bb.configuration(1, [3, N, 2], precision=prec)
-            got = run(bb, torch_cuda, cfg, x.ravel(), X.size, X.dtype)
+            got = run(bb, torch_cuda, cfg, x.ravel().astype(cdt), X.size, cdt)
             assert approx_ok(got.reshape(X.shape), X, po.tol(prec, N)), (prec, N)
         for N in (16, 27):
             x, X = z[f'r2c_{prec}_{N}_x'], z[f'r2c_{prec}_{N}_X']
             cfg = bb.configuration(1, [2, N, 3], precision=prec, type=bb.R2C)
-            got = run(bb, torch_cuda, cfg, x.ravel(), X.size, X.dtype)
+            got = run(bb, torch_cuda, cfg, x.ravel().astype(rdt), X.size, cdt)
             assert approx_ok(got.reshape(X.shape), X, po.tol(prec, N)), (prec, N)
         X, y = z[f'c2r_{prec}_48_X'], z[f'c2r_{prec}_48_y']
         cfg = bb.configuration(1, [2, 48, 3], precision=prec, type=bb.C2R, direction=bb.BACKWARD)
-        got = run(bb, torch_cuda, cfg, X.ravel(), y.size, y.dtype)
+        got = run(bb, torch_cuda, cfg, X.ravel().astype(cdt), y.size, rdt)
         assert approx_ok(got.reshape(y.shape), y, po.tol(prec, 48)), prec
