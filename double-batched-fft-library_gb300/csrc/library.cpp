@@ -469,18 +469,23 @@ static int max_optin_smem(int device) {
 // The dynamic shared-memory limit is a property of the kernel, shared by every plan that
 // launches it: raise it once per kernel and device to the device maximum (lowering it for
 // one plan would break the launches of another).
-static void allow_max_smem(const void *func, int device) {
+// Raise a kernel's dynamic shared-memory limit to the device maximum.  Kernels compiled
+// into the library are set once per device; kernels of NVRTC modules (module_kernel) are
+// set every time, since a handle of an unloaded module can be reused by a new one.
+static void allow_max_smem(const void *func, int device, bool module_kernel = false) {
     static std::mutex mu;
     static std::set<std::pair<const void *, int>> done;
     std::lock_guard<std::mutex> lock(mu);
-    if (done.count({func, device})) {
+    if (!module_kernel && done.count({func, device})) {
         return;
     }
     cudaFuncAttributes attr;
     GB_CUDA(cudaFuncGetAttributes(&attr, func));
     GB_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  max_optin_smem(device) - static_cast<int>(attr.sharedSizeBytes)));
-    done.insert({func, device});
+    if (!module_kernel) {
+        done.insert({func, device});
+    }
 }
 
 static std::string c_ident(std::string s) {
@@ -1075,7 +1080,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         ps.func = reinterpret_cast<const void *>(k);
     }
     if (smem > 48 * 1024) {
-        allow_max_smem(ps.func, device);
+        allow_max_smem(ps.func, device, static_cast<bool>(ps.mod));
     }
     return ps;
 }
