@@ -22,7 +22,10 @@ LIB = os.path.join(OUTDIR, 'libbbfft_gb300.so')
 
 ARCH = '-gencode=arch=compute_103a,code=sm_103a'
 ENGINE_HEADERS = ['params.h', 'root_of_unity_table.cuh', 'radix.cuh', 'engine.cuh']
-KERNEL_UNITS = ['kernels_f32.cu', 'kernels_f64.cu', 'noalloc.cu', 'ragged.cu', 'tc.cu']
+KERNEL_UNITS = ['kernels_f32.cu', 'kernels_f64.cu', 'noalloc.cu', 'tc.cu']
+# relocatable device code, linked with nvcc -dlink: the persistent ragged kernel calls the
+# compile-time-size tile functions of the generated ragged_ct_<i>.cu units
+RDC_UNITS = ['ragged.cu']
 HOST_UNITS = ['library.cpp', 'config.cpp']
 
 
@@ -83,12 +86,23 @@ def build(verbose=False, jobs=None):
     cuda = cuda_home()
     nvcc = os.path.join(cuda, 'bin', 'nvcc')
     embed_engine()
-    gen_units = generate_specializations()
+    gen_units, rag_units = generate_specializations()
     headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC)
                if h.endswith(('.h', '.hpp', '.cuh'))] + [os.path.join(INCLUDE, 'bbfft_gb300.h')]
-    common_inc = ['-I' + CSRC, '-I' + INCLUDE, '-I' + BUILD, '-I' + os.path.join(cuda, 'include')]
+    common_inc = ['-I' + CSRC, '-I' + INCLUDE, '-I' + BUILD, '-I' + os.path.join(BUILD, 'gen'),
+                  '-I' + os.path.join(cuda, 'include')]
     jobs_list = []
     objs = []
+    rdc_objs = []
+    for src in [os.path.join(CSRC, u) for u in RDC_UNITS] + rag_units:
+        u = os.path.basename(src)
+        obj = os.path.join(BUILD, u + '.o')
+        rdc_objs.append(obj)
+        deps = [src] + headers + [os.path.join(BUILD, 'gen', 'ragged_ct_dispatch.inc')]
+        if newer(obj, deps):
+            jobs_list.append([nvcc, ARCH, '-lineinfo', '-O3', '-std=c++17', '-rdc=true',
+                              '-maxrregcount=128', '-Xcompiler', '-fPIC', '-Xcompiler',
+                              '-fvisibility=hidden', '-Xptxas', '-v', '-c', src, '-o', obj] + common_inc)
     for src in [os.path.join(CSRC, u) for u in KERNEL_UNITS] + gen_units:
         u = os.path.basename(src)
         obj = os.path.join(BUILD, u + '.o')
@@ -111,6 +125,10 @@ def build(verbose=False, jobs=None):
         if verbose:
             for o in outs:
                 sys.stdout.write(o)
+    dlink = os.path.join(BUILD, 'ragged_dlink.o')
+    if newer(dlink, rdc_objs):
+        run([nvcc, ARCH, '-dlink', '-Xcompiler', '-fPIC', '-o', dlink] + rdc_objs)
+    objs += rdc_objs + [dlink]
     if newer(LIB, objs):
         run([nvcc, ARCH, '-shared', '-Xcompiler', '-fPIC', '-o', LIB] + objs +
             ['-L' + os.path.join(cuda, 'lib64'), '-lcudart', '-lnvrtc'])

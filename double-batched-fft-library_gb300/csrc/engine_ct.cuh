@@ -101,9 +101,12 @@ template <int V> __device__ __forceinline__ void stv(double *p, const double *o)
     }
 }
 
-template <class R, int Kind, int NC, int TT, int V> struct ct_ctx {
+template <class R, int Kind, int NC, int TT, int V, bool MI = false> struct ct_ctx {
     using C = cplx<R>;
     static constexpr int kind_v = Kind;
+    // may_idle: the block has more threads than the tile (persistent ragged kernel); the
+    // threads beyond the tile (live == false) only take part in the barriers
+    static constexpr bool may_idle = MI;
     static constexpr bool half = Kind == kind_r2c_half || Kind == kind_c2r_half;
     static constexpr int NN = half ? 2 * NC : NC; // logical length (odd kinds: N = NC)
     // lane vectors of 16 bytes or more are stored as 16-byte chunks in NQ planes with an
@@ -117,6 +120,7 @@ template <class R, int Kind, int NC, int TT, int V> struct ct_ctx {
     int sbase; // LIN: shared index of element 0; else chunk index of element 0
     int pshift, padd;
     bool active;
+    bool live = true;
 
     __device__ __forceinline__ int sidx(int n) const { // LIN layout
         int i = sbase + n * p.Mb;
@@ -284,7 +288,7 @@ __device__ __forceinline__ void ct_stage(const Ctx &c, int j) {
 #pragma unroll
     for (int it = 0; it < ITERS; ++it) {
         const int b = j + it * TT;
-        if (nb % TT == 0 || b < nb) {
+        if ((nb % TT == 0 || b < nb) && (!Ctx::may_idle || c.live)) {
             if constexpr (SRC_G) {
                 if (c.active) {
                     sfor<0, P>([&](auto I) {
@@ -320,7 +324,7 @@ __device__ __forceinline__ void ct_stage(const Ctx &c, int j) {
 #pragma unroll
     for (int it = 0; it < ITERS; ++it) {
         const int b = j + it * TT;
-        if (nb % TT == 0 || b < nb) {
+        if ((nb % TT == 0 || b < nb) && (!Ctx::may_idle || c.live)) {
             const int o = b + (b / NS) * NS * (P - 1);
             sfor<0, P>([&](auto I) {
                 C t[V];
@@ -344,6 +348,11 @@ __device__ __forceinline__ void ct_r2c_post(const Ctx &c, int j) {
     const C *tw = static_cast<const C *>(c.p.tw);
     constexpr int cnt = NC / 2 + 1;
     constexpr int ITERS = (cnt + TT - 1) / TT;
+    if constexpr (Ctx::may_idle) {
+        if (!c.live) {
+            return;
+        }
+    }
     R g0[V];
     if (c.p.flags & flag_adj_c2r) {
         C z0[V];
@@ -419,6 +428,29 @@ __device__ __forceinline__ void fft_tile_ct(const fft_params &p) {
     const int sbase = Ctx::LIN ? k_l * NC * p.Mb + m_l : k_l * NC * mvb + mv;
     Ctx c{p, reinterpret_cast<cplx<R> *>(smem_raw), m + k * p.is2, m + k * p.os2, sbase,
           p.pad_shift, p.pad_add, (m < p.M) && (k < p.K)};
+    ct_run<Ctx, R, NC, TT, V, 0, sizeof...(Ps), 1, Ps...>(c, j);
+}
+
+// The same tile for the persistent ragged kernel: tile index given, block possibly larger
+// than the tile's (Mb / V) * TT * Kb threads.
+template <class R, int Kind, int NC, int TT, int V, int... Ps>
+__device__ __forceinline__ void fft_tile_ct_ragged(const fft_params &p, long long tile) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    using Ctx = ct_ctx<R, Kind, NC, TT, V, true>;
+    const int tid = threadIdx.x;
+    const int mvb = p.Mb / V;
+    const bool live = tid < mvb * TT * p.Kb;
+    const int mv = tid % mvb;
+    const int j = (tid / mvb) % TT;
+    const int k_l = live ? tid / (mvb * TT) : 0;
+    const long long mt = tile % p.m_tiles;
+    const long long kt = tile / p.m_tiles;
+    const int m_l = mv * V;
+    const long long m = mt * p.Mb + m_l;
+    const long long k = kt * p.Kb + k_l;
+    const int sbase = Ctx::LIN ? k_l * NC * p.Mb + m_l : k_l * NC * mvb + mv;
+    Ctx c{p, reinterpret_cast<cplx<R> *>(smem_raw), m + k * p.is2, m + k * p.os2, sbase,
+          p.pad_shift, p.pad_add, live && (m < p.M) && (k < p.K), live};
     ct_run<Ctx, R, NC, TT, V, 0, sizeof...(Ps), 1, Ps...>(c, j);
 }
 

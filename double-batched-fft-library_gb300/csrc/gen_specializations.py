@@ -114,6 +114,85 @@ def entries():
     return out
 
 
+# Ragged batches: float c2c N = 16..512 step 8 and r2c N = 16..512 step 8 (half length
+# 8..256 step 4), one thread per M (V = 1), as device functions of the persistent kernel.
+RAGGED_FILES = 4
+
+
+def ragged_entries():
+    out = []
+    for kind, ncs in ((0, range(16, 513, 8)), (1, range(8, 257, 4))):
+        for nc in ncs:
+            rad, T = stage_list(nc, kind)
+            if any(r not in UNROLLED for r in rad):
+                continue
+            out.append((4, kind, nc, T, rad, 1))
+    return out
+
+
+def write(fn, text):
+    if not os.path.exists(fn) or open(fn).read() != text:
+        with open(fn, 'w') as f:
+            f.write(text)
+
+
+def ragged_units(outdir):
+    """ragged_ct_<i>.cu (the variant functions, spread over RAGGED_FILES units),
+    ragged_ct_dispatch.inc (declarations and the switch, included by ragged.cu) and the
+    host table lines for ct_index.cpp."""
+    ents = ragged_entries()
+    cost = lambda e: e[2] * len(e[4])
+    order = sorted(range(len(ents)), key=lambda i: -cost(ents[i]))
+    groups = [[] for _ in range(RAGGED_FILES)]
+    load = [0] * RAGGED_FILES
+    for i in order:
+        g = load.index(min(load))
+        groups[g].append(i)
+        load[g] += cost(ents[i])
+    units = []
+    for g, idx in enumerate(groups):
+        src = ['// generated by gen_specializations.py: compile-time-size tiles of the ragged kernel',
+               '#include "engine_ct.cuh"', '#include "kernels.hpp"', '', 'namespace gbfft {', '']
+        for i in sorted(idx):
+            prec, kind, nc, T, rad, V = ents[i]
+            src += ['__device__ __noinline__ void ragged_ct_%d(const fft_params &p, long long tile) {' % i,
+                    '    fft_tile_ct_ragged<float, %d, %d, %d, %d, %s>(p, tile);' % (kind, nc, T, V, ', '.join(map(str, rad))),
+                    '}', '']
+        src += ['} // namespace gbfft', '']
+        fn = os.path.join(outdir, 'ragged_ct_%d.cu' % g)
+        write(fn, '\n'.join(src))
+        units.append(fn)
+    inc = ['// generated by gen_specializations.py: compile-time-size ragged tiles', '']
+    inc += ['__device__ void ragged_ct_%d(const fft_params &p, long long tile);' % i for i in range(len(ents))]
+    inc += ['', '__device__ __forceinline__ void ragged_ct_call(int vid, const fft_params &p, long long tile) {',
+            '    switch (vid) {']
+    for i in range(len(ents)):
+        inc += ['    case %d:' % i, '        ragged_ct_%d(p, tile);' % i, '        break;']
+    inc += ['    }', '}', '']
+    write(os.path.join(outdir, 'ragged_ct_dispatch.inc'), '\n'.join(inc))
+    host = ['extern const ct_entry ragged_ct_table[] = {']
+    for prec, kind, nc, T, rad, V in ents:
+        host.append('    {%d, %d, %d, %d, %d, %d, {%s}, nullptr},' % (prec, kind, nc, T, V, len(rad), ', '.join(map(str, rad))))
+    host += ['};', 'static const int kRaggedSize = %d;' % len(ents), '',
+             'int ragged_ct_lookup(int prec, int kind, int nc, int T, int V, const int *rad, int L) {',
+             '    for (int i = 0; i < kRaggedSize; ++i) {',
+             '        const ct_entry &e = ragged_ct_table[i];',
+             '        if (e.prec != prec || e.kind != kind || e.nc != nc || e.T != T || e.V != V || e.L != L) {',
+             '            continue;',
+             '        }',
+             '        bool same = true;',
+             '        for (int s = 0; s < L; ++s) {',
+             '            same = same && e.rad[s] == rad[s];',
+             '        }',
+             '        if (same) {',
+             '            return i;',
+             '        }',
+             '    }',
+             '    return -1;',
+             '}', '']
+    return units, host
+
+
 def main(outdir):
     os.makedirs(outdir, exist_ok=True)
     ents = entries()
@@ -165,14 +244,18 @@ def main(outdir):
               '        }',
               '    }',
               '    return nullptr;',
-              '}', '', '} // namespace gbfft', '']
+              '}', '']
+    rag_units, rag_host = ragged_units(outdir)
+    index += rag_host + ['} // namespace gbfft', '']
     fn = os.path.join(outdir, 'ct_index.cpp')
     text = '\n'.join(index)
     if not os.path.exists(fn) or open(fn).read() != text:
         with open(fn, 'w') as f:
             f.write(text)
-    return sorted(os.path.join(outdir, 'kernels_ct_f%d_%s.cu' % (p * 8, KINDS[k])) for p, k in files)
+    return (sorted(os.path.join(outdir, 'kernels_ct_f%d_%s.cu' % (p * 8, KINDS[k])) for p, k in files),
+            rag_units)
 
 
 if __name__ == '__main__':
-    print('\n'.join(main(sys.argv[1])))
+    ct_units, rag_units = main(sys.argv[1])
+    print('\n'.join(ct_units + rag_units))

@@ -21,6 +21,9 @@ struct ct_entry {
     const void *fn;
 };
 const ct_entry *ct_lookup(int prec, int kind, int nc, int T, int V, const int *rad, int L);
+// compile-time-size tiles of the persistent ragged kernel: index into ragged_ct_table or -1
+extern const ct_entry ragged_ct_table[];
+int ragged_ct_lookup(int prec, int kind, int nc, int T, int V, const int *rad, int L);
 
 // tensor-core DFT stages (tc.cu)
 const void *tc_kernel(int pieces, int nc);

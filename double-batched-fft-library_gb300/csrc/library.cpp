@@ -388,6 +388,7 @@ struct pass {
     bool tc = false;          // tensor-core DFT stages
     int V = 1;                // transforms per thread along M
     std::shared_ptr<pass> scalar_alt; // V = 1 variant for pointers not aligned to 16 bytes
+    int ragged_vid = -1;              // compile-time-size tile of the ragged kernel, or -1
     std::string identifier;
     int in_sel = 0;  // 0: user input, 2: temporary
     int out_sel = 1; // 1: user output, 2: temporary
@@ -915,6 +916,14 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
             ct = ct_lookup(q.prec, ps.kind, Nc, T, 1, rad.data(), L);
         }
     }
+    // ragged batches: compile-time-size tile functions of the persistent kernel (float, V = 1)
+    int ragged_vid = -1;
+    if (!has_cb && q.runtime_only && q.prec == 4) {
+        ragged_vid = ragged_ct_lookup(q.prec, ps.kind, Nc, T, 1, rad.data(), L);
+        if (ragged_vid >= 0) {
+            ct = &ragged_ct_table[ragged_vid];
+        }
+    }
     int const max_block = q.max_block > 0 ? q.max_block : (ct ? 256 : 512);
     // the runtime kernel ping-pongs between two buffers when a stage goes shared->shared;
     // compile-time kernels run their stages in place in one buffer
@@ -1042,8 +1051,9 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     ps.identifier = c_ident(id.str());
 
     if (!has_cb) {
-        ps.func = ct ? ct->fn : (q.prec == 4 ? kernel_f32(ps.kind) : kernel_f64(ps.kind));
+        ps.func = (ct && ct->fn) ? ct->fn : (q.prec == 4 ? kernel_f32(ps.kind) : kernel_f64(ps.kind));
         ps.specialized = ct != nullptr;
+        ps.ragged_vid = ragged_vid;
         if (V > 1) {
             pass_request q1 = q;
             q1.force_v1 = true;
@@ -1553,6 +1563,7 @@ static void make_ragged(bbfft_ragged_item const *items, std::size_t n, bbfft_rag
         dev[i].p.in = it.in;
         dev[i].p.out = it.out;
         dev[i].kind = ps.kind;
+        dev[i].vid = ps.ragged_vid;
         smem = std::max(smem, ps.smem);
         std::size_t ib = it.type == BBFFT_R2C ? it.precision : 2 * it.precision;
         std::size_t ob = it.type == BBFFT_C2R ? it.precision : 2 * it.precision;

@@ -62,7 +62,7 @@ namespace gbfft {
 struct ragged_item_dev {
     fft_params p;
     int kind;
-    int pad_;
+    int vid; // compile-time-size tile function (ragged_ct_call), or -1: runtime-size engine
 };
 
 } // namespace gbfft

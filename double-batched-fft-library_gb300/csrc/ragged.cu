@@ -9,17 +9,23 @@
 // The reference launches one kernel per plan (src/common/algorithm/small_batch_fft.hpp:111);
 // it has no ragged form.
 #include "engine.cuh"
+#include "engine_ct.cuh"
 #include "kernels.hpp"
 
 namespace gbfft {
 
+// ragged_ct_call(vid, p, tile): the compile-time-size tile functions (generated units,
+// linked as relocatable device code)
+#include "ragged_ct_dispatch.inc"
+
 template <class R>
-__global__ void __launch_bounds__(256) ragged_kernel(const ragged_item_dev *__restrict__ items,
+__global__ void __launch_bounds__(256, 2) ragged_kernel(const ragged_item_dev *__restrict__ items,
                                                      const int2 *__restrict__ units, int n_units,
                                                      unsigned *counter) {
     __shared__ int s_unit;
     __shared__ __align__(16) fft_params s_p;
     __shared__ int s_kind;
+    __shared__ int s_vid;
     for (;;) {
         if (threadIdx.x == 0) {
             s_unit = static_cast<int>(atomicAdd(counter, 1u));
@@ -37,24 +43,31 @@ __global__ void __launch_bounds__(256) ragged_kernel(const ragged_item_dev *__re
         }
         if (threadIdx.x == 0) {
             s_kind = items[un.x].kind;
+            s_vid = items[un.x].vid;
         }
         __syncthreads();
-        switch (s_kind) {
-        case kind_c2c:
-            fft_tile_at<R, kind_c2c, default_io>(s_p, un.y);
-            break;
-        case kind_r2c_half:
-            fft_tile_at<R, kind_r2c_half, default_io>(s_p, un.y);
-            break;
-        case kind_r2c_full:
-            fft_tile_at<R, kind_r2c_full, default_io>(s_p, un.y);
-            break;
-        case kind_c2r_half:
-            fft_tile_at<R, kind_c2r_half, default_io>(s_p, un.y);
-            break;
-        case kind_c2r_full:
-            fft_tile_at<R, kind_c2r_full, default_io>(s_p, un.y);
-            break;
+        if (s_vid >= 0) {
+            if constexpr (sizeof(R) == 4) {
+                ragged_ct_call(s_vid, s_p, un.y);
+            }
+        } else {
+            switch (s_kind) {
+            case kind_c2c:
+                fft_tile_at<R, kind_c2c, default_io>(s_p, un.y);
+                break;
+            case kind_r2c_half:
+                fft_tile_at<R, kind_r2c_half, default_io>(s_p, un.y);
+                break;
+            case kind_r2c_full:
+                fft_tile_at<R, kind_r2c_full, default_io>(s_p, un.y);
+                break;
+            case kind_c2r_half:
+                fft_tile_at<R, kind_c2r_half, default_io>(s_p, un.y);
+                break;
+            case kind_c2r_full:
+                fft_tile_at<R, kind_c2r_full, default_io>(s_p, un.y);
+                break;
+            }
         }
         __syncthreads(); // shared memory and s_p are reused by the next unit
     }
