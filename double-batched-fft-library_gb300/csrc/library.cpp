@@ -1616,7 +1616,6 @@ static void make_ragged(bbfft_ragged_item const *items, std::size_t n, bbfft_rag
 }
 
 static void launch_ragged(bbfft_ragged_s &r, cudaStream_t stream) {
-    GB_CUDA(cudaMemsetAsync(r.counter->ptr, 0, sizeof(unsigned), stream));
     const void *items = r.items->ptr;
     const void *units = r.units->ptr;
     int n = r.n_units;
