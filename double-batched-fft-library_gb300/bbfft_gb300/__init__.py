@@ -152,6 +152,7 @@ _SIGNATURES = {
                                            ctypes.POINTER(_vp)]),
     'bbfft_ragged_execute': (ctypes.c_int, [_vp, _vp, ctypes.c_int]),
     'bbfft_ragged_get_info': (ctypes.c_int, [_vp, ctypes.POINTER(RaggedInfo)]),
+    'bbfft_ragged_set_launch_form': (ctypes.c_int, [_vp, ctypes.c_int]),
     'bbfft_ragged_destroy': (ctypes.c_int, [_vp]),
     'bbfft_c2r_2d_noalloc_f32': (ctypes.c_int, [_vp, _vp, ctypes.c_size_t, ctypes.c_size_t,
                                                 ctypes.c_size_t, ctypes.c_size_t, _vp]),
@@ -345,7 +346,7 @@ class Plan:
 
 
 class Ragged:
-    """A ragged batch of independent 1d transforms run by one persistent launch.
+    """A ragged batch of independent 1d transforms run by one kernel launch.
 
     items: list of (precision, direction, type, N, M, K, in_ptr, out_ptr) with default
     packed layouts (include/bbfft_gb300.h: bbfft_ragged_item)."""
@@ -358,8 +359,15 @@ class Ragged:
         _check(lib().bbfft_ragged_create(arr, len(items), ctypes.byref(h)))
         self.handle = h
 
+    PERSISTENT, GRID = 0, 1
+
     def execute(self, stream=None, use_graph=False):
         _check(lib().bbfft_ragged_execute(self.handle, _stream_ptr(stream), int(bool(use_graph))))
+
+    def set_launch_form(self, form):
+        """Ragged.PERSISTENT (CTAs take tiles from a counter) or Ragged.GRID (one CTA per
+        tile); include/bbfft_gb300.h: bbfft_ragged_set_launch_form."""
+        _check(lib().bbfft_ragged_set_launch_form(self.handle, int(form)))
 
     def info(self):
         i = RaggedInfo()

@@ -31,6 +31,6 @@ std::size_t tc_shared_bytes();
 int tc_tile_transforms(int nc);
 
 // persistent kernel of ragged batches (ragged.cu)
-const void *ragged_kernel_ptr(int prec);
+const void *ragged_kernel_ptr(int prec, bool persistent);
 
 } // namespace gbfft

@@ -1490,7 +1490,9 @@ struct bbfft_ragged_s {
     int n_units = 0;
     unsigned grid = 0, block = 256;
     std::size_t smem = 0;
-    const void *func = nullptr;
+    const void *func = nullptr;      // persistent kernel
+    const void *grid_func = nullptr; // one CTA per unit
+    int form = BBFFT_RAGGED_PERSISTENT;
     uint64_t bytes = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -1593,11 +1595,13 @@ static void make_ragged(bbfft_ragged_item const *items, std::size_t n, bbfft_rag
                        cudaMemcpyHostToDevice));
     GB_CUDA(cudaMemcpy(r.units->ptr, flat.data(), flat.size() * sizeof(int),
                        cudaMemcpyHostToDevice));
-    r.func = ragged_kernel_ptr(r.prec);
+    r.func = ragged_kernel_ptr(r.prec, true);
+    r.grid_func = ragged_kernel_ptr(r.prec, false);
     r.block = block;
     r.smem = smem;
     if (smem > 48 * 1024) {
         allow_max_smem(r.func, r.device);
+        allow_max_smem(r.grid_func, r.device);
     }
     int per_sm = 0, sms = 0;
     GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, r.func, block, smem));
@@ -1621,6 +1625,12 @@ static void launch_ragged(bbfft_ragged_s &r, cudaStream_t stream) {
     int n = r.n_units;
     void *counter = r.counter->ptr;
     void *args[] = {&items, &units, &n, &counter};
+    if (r.form == BBFFT_RAGGED_GRID) {
+        GB_CUDA(cudaLaunchKernel(r.grid_func, dim3(static_cast<unsigned>(std::max(1, n))),
+                                 dim3(r.block), args, r.smem, stream));
+        return;
+    }
+    GB_CUDA(cudaMemsetAsync(r.counter->ptr, 0, sizeof(unsigned), stream));
     GB_CUDA(cudaLaunchKernel(r.func, dim3(r.grid), dim3(r.block), args, r.smem, stream));
 }
 
@@ -1986,6 +1996,25 @@ int bbfft_ragged_execute(bbfft_ragged_t ragged, cudaStream_t stream, int use_gra
             GB_CUDA(cudaGraphInstantiate(&ragged->exec, ragged->graph, 0));
         }
         GB_CUDA(cudaGraphLaunch(ragged->exec, stream));
+    });
+}
+
+int bbfft_ragged_set_launch_form(bbfft_ragged_t ragged, int form) {
+    return guarded([&] {
+        if (!ragged || (form != BBFFT_RAGGED_PERSISTENT && form != BBFFT_RAGGED_GRID)) {
+            throw status_error(BBFFT_INVALID_ARGUMENT, "null ragged batch or unknown launch form");
+        }
+        if (form != ragged->form) {
+            ragged->form = form;
+            if (ragged->exec) { // the captured graph holds the other form
+                cudaGraphExecDestroy(ragged->exec);
+                ragged->exec = nullptr;
+            }
+            if (ragged->graph) {
+                cudaGraphDestroy(ragged->graph);
+                ragged->graph = nullptr;
+            }
+        }
     });
 }
 

@@ -2,10 +2,9 @@
 // lengths, kinds and batch sizes in ONE launch.
 //
 // The host splits every transform into CTA tiles ("units"), orders the units largest
-// first and stores them in a table.  Persistent CTA b runs units b, b + G, b + 2G, ...
-// (G CTAs; no CTA ever waits on another), with the parameters of the next unit fetched
-// while the current one runs, and each unit on its compile-time-size tile function when
-// one exists, else on the runtime-size engine.
+// first and stores them in a table.  A unit runs on its compile-time-size tile function
+// when one exists, else on the runtime-size engine.  Two launch forms share the table:
+// persistent CTAs taking units from a counter, or one CTA per unit.
 // The reference launches one kernel per plan (src/common/algorithm/small_batch_fft.hpp:111);
 // it has no ragged form.
 #include "engine.cuh"
@@ -18,96 +17,90 @@ namespace gbfft {
 // linked as relocatable device code)
 #include "ragged_ct_dispatch.inc"
 
+// One unit: its parameters staged in shared memory, then its tile.
+template <class R>
+__device__ __forceinline__ void ragged_unit(const ragged_item_dev *__restrict__ items, int2 un,
+                                            fft_params &s_p, int &s_kind, int &s_vid) {
+    constexpr int NW = static_cast<int>(sizeof(fft_params) / sizeof(int));
+    const int tid = threadIdx.x;
+    if (tid < NW) {
+        reinterpret_cast<int *>(&s_p)[tid] = __ldg(reinterpret_cast<const int *>(&items[un.x].p) + tid);
+    }
+    if (tid == 0) {
+        s_kind = items[un.x].kind;
+        s_vid = items[un.x].vid;
+    }
+    __syncthreads();
+    if (s_vid >= 0) {
+        if constexpr (sizeof(R) == 4) {
+            ragged_ct_call(s_vid, s_p, un.y);
+        }
+    } else {
+        switch (s_kind) {
+        case kind_c2c:
+            fft_tile_at<R, kind_c2c, default_io>(s_p, un.y);
+            break;
+        case kind_r2c_half:
+            fft_tile_at<R, kind_r2c_half, default_io>(s_p, un.y);
+            break;
+        case kind_r2c_full:
+            fft_tile_at<R, kind_r2c_full, default_io>(s_p, un.y);
+            break;
+        case kind_c2r_half:
+            fft_tile_at<R, kind_c2r_half, default_io>(s_p, un.y);
+            break;
+        case kind_c2r_full:
+            fft_tile_at<R, kind_c2r_full, default_io>(s_p, un.y);
+            break;
+        }
+    }
+}
+
+// Persistent form: G CTAs; each takes the next unit from a device counter (one atomicAdd
+// by one thread; no thread waits on another CTA) until the table is exhausted.  The
+// counter is reset before every launch.
 template <class R>
 __global__ void __launch_bounds__(256, 2) ragged_kernel(const ragged_item_dev *__restrict__ items,
                                                      const int2 *__restrict__ units, int n_units,
                                                      unsigned *counter) {
-    (void)counter;
-    constexpr int NW = static_cast<int>(sizeof(fft_params) / sizeof(int));
-    static_assert(NW <= 256, "parameter block larger than the block");
-    __shared__ __align__(16) fft_params s_p[2];
-    __shared__ int s_kind[2], s_vid[2];
-    __shared__ long long s_tile[2];
-    const int tid = threadIdx.x;
-    const int G = gridDim.x;
-    int u = blockIdx.x;
-    if (u >= n_units) {
-        return;
-    }
-    {
-        const int2 un = units[u];
-        if (tid < NW) {
-            reinterpret_cast<int *>(&s_p[0])[tid] = reinterpret_cast<const int *>(&items[un.x].p)[tid];
+    static_assert(sizeof(fft_params) / sizeof(int) <= 256, "parameter block larger than the block");
+    __shared__ int s_unit;
+    __shared__ __align__(16) fft_params s_p;
+    __shared__ int s_kind, s_vid;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_unit = static_cast<int>(atomicAdd(counter, 1u));
         }
-        if (tid == 0) {
-            s_kind[0] = items[un.x].kind;
-            s_vid[0] = items[un.x].vid;
-            s_tile[0] = un.y;
-        }
-    }
-    __syncthreads();
-    for (int slot = 0;; slot ^= 1) {
-        // the units of a block are u, u + G, u + 2G, ... (LPT order, round robin): the
-        // parameters of the next one are loaded into registers before this tile runs and
-        // stored into the other slot after it, so no tile waits for them
-        const int un_i = u + G;
-        const bool more = un_i < n_units;
-        int pw = 0, nk = 0, nv = 0;
-        long long nt = 0;
-        if (more) {
-            const int2 un = units[un_i];
-            if (tid < NW) {
-                pw = __ldg(reinterpret_cast<const int *>(&items[un.x].p) + tid);
-            }
-            if (tid == 0) {
-                nk = __ldg(&items[un.x].kind);
-                nv = __ldg(&items[un.x].vid);
-                nt = un.y;
-            }
-        }
-        const fft_params &p = s_p[slot];
-        if (s_vid[slot] >= 0) {
-            if constexpr (sizeof(R) == 4) {
-                ragged_ct_call(s_vid[slot], p, s_tile[slot]);
-            }
-        } else {
-            switch (s_kind[slot]) {
-            case kind_c2c:
-                fft_tile_at<R, kind_c2c, default_io>(p, s_tile[slot]);
-                break;
-            case kind_r2c_half:
-                fft_tile_at<R, kind_r2c_half, default_io>(p, s_tile[slot]);
-                break;
-            case kind_r2c_full:
-                fft_tile_at<R, kind_r2c_full, default_io>(p, s_tile[slot]);
-                break;
-            case kind_c2r_half:
-                fft_tile_at<R, kind_c2r_half, default_io>(p, s_tile[slot]);
-                break;
-            case kind_c2r_full:
-                fft_tile_at<R, kind_c2r_full, default_io>(p, s_tile[slot]);
-                break;
-            }
-        }
-        if (!more) {
+        __syncthreads();
+        const int u = s_unit;
+        if (u >= n_units) {
             return;
         }
-        if (tid < NW) {
-            reinterpret_cast<int *>(&s_p[slot ^ 1])[tid] = pw;
-        }
-        if (tid == 0) {
-            s_kind[slot ^ 1] = nk;
-            s_vid[slot ^ 1] = nv;
-            s_tile[slot ^ 1] = nt;
-        }
-        __syncthreads(); // the next tile's parameters are visible; shared data is free
-        u = un_i;
+        ragged_unit<R>(items, units[u], s_p, s_kind, s_vid);
+        __syncthreads(); // shared memory and s_p are reused by the next unit
     }
 }
 
-const void *ragged_kernel_ptr(int prec) {
-    return prec == 4 ? reinterpret_cast<const void *>(&ragged_kernel<float>)
-                     : reinterpret_cast<const void *>(&ragged_kernel<double>);
+// Grid form: one CTA per unit, scheduled by the hardware (same unit table and tiles).
+template <class R>
+__global__ void __launch_bounds__(256, 2) ragged_grid_kernel(const ragged_item_dev *__restrict__ items,
+                                                          const int2 *__restrict__ units, int n_units,
+                                                          unsigned *counter) {
+    (void)counter;
+    __shared__ __align__(16) fft_params s_p;
+    __shared__ int s_kind, s_vid;
+    if (static_cast<int>(blockIdx.x) < n_units) {
+        ragged_unit<R>(items, units[blockIdx.x], s_p, s_kind, s_vid);
+    }
+}
+
+const void *ragged_kernel_ptr(int prec, bool persistent) {
+    if (persistent) {
+        return prec == 4 ? reinterpret_cast<const void *>(&ragged_kernel<float>)
+                         : reinterpret_cast<const void *>(&ragged_kernel<double>);
+    }
+    return prec == 4 ? reinterpret_cast<const void *>(&ragged_grid_kernel<float>)
+                     : reinterpret_cast<const void *>(&ragged_grid_kernel<double>);
 }
 
 } // namespace gbfft

@@ -235,10 +235,17 @@ typedef struct bbfft_ragged_info {
 /* Plans all transforms of the batch for ONE persistent launch on the current device. */
 BBFFT_GB300_API int bbfft_ragged_create(const bbfft_ragged_item *items, size_t num_items,
                                         bbfft_ragged_t *ragged);
-/* Runs the whole batch: a reset of the work counter and one persistent kernel.  With
- * use_graph != 0 both are captured once into a CUDA graph that is replayed on `stream`. */
+/* Runs the whole batch in one kernel launch.  Persistent form (default): a reset of the
+ * work counter and one persistent kernel whose CTAs take tiles from the counter.  Grid
+ * form: one CTA per tile.  With use_graph != 0 the launch is captured once into a CUDA
+ * graph that is replayed on `stream`. */
 BBFFT_GB300_API int bbfft_ragged_execute(bbfft_ragged_t ragged, cudaStream_t stream,
                                          int use_graph);
+#define BBFFT_RAGGED_PERSISTENT 0
+#define BBFFT_RAGGED_GRID 1
+/* Selects the launch form of bbfft_ragged_execute (BBFFT_RAGGED_PERSISTENT or
+ * BBFFT_RAGGED_GRID); drops a graph captured for the other form. */
+BBFFT_GB300_API int bbfft_ragged_set_launch_form(bbfft_ragged_t ragged, int form);
 BBFFT_GB300_API int bbfft_ragged_get_info(bbfft_ragged_t ragged, bbfft_ragged_info *info);
 BBFFT_GB300_API int bbfft_ragged_destroy(bbfft_ragged_t ragged);
 

@@ -1,5 +1,6 @@
 """Ragged batches: many independent 1d transforms of mixed N, kind and batch sizes in one
-persistent launch (optionally replayed from a CUDA graph), against the FP64 DFT."""
+launch (persistent CTAs or one CTA per tile, optionally replayed from a CUDA graph),
+against the FP64 DFT."""
 import numpy as np
 import pytest
 
@@ -50,11 +51,13 @@ def check_items(bb, po, specs, x, y, idx):
     return worst
 
 
+@pytest.mark.parametrize('form', [0, 1])
 @pytest.mark.parametrize('use_graph', [False, True])
-def test_ragged_small_batch(bb, po, torch_cuda, use_graph):
+def test_ragged_small_batch(bb, po, torch_cuda, use_graph, form):
     torch = torch_cuda
     specs, x, y, items = make_batch(bb, torch, 300, seed=11)
     r = bb.Ragged(items)
+    r.set_launch_form(form)
     info = r.info()
     assert info.num_units >= len(items) and info.grid >= 1
     r.execute(torch.cuda.current_stream().cuda_stream, use_graph=use_graph)
@@ -73,6 +76,12 @@ def test_ragged_benchmark_batch_graph_replay(bb, po, torch_cuda):
     torch.cuda.synchronize()
     first = y.clone()
     y.zero_()
+    r.execute(s, use_graph=True)
+    torch.cuda.synchronize()
+    assert torch.equal(first, y)
+    # the grid form (one CTA per tile) computes the same tiles with the same code
+    y.zero_()
+    r.set_launch_form(r.GRID)
     r.execute(s, use_graph=True)
     torch.cuda.synchronize()
     assert torch.equal(first, y)
