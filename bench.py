@@ -423,8 +423,9 @@ def ragged_specs(bb, n=10000, seed=4):
 
 
 def leg_ragged(bb, torch, stream, hbm_peak, steps, warmup):
-    """10^4 transforms with U[-1,1] data in one launch replayed from a graph: persistent
-    CTAs taking tiles from a counter, and one CTA per tile."""
+    """10^4 transforms with U[-1,1] data replayed from a graph: one launch (persistent CTAs
+    taking tiles from a counter, or one CTA per tile) and one kernel node per tile
+    function (class form)."""
     specs, nin, nout = ragged_specs(bb)
     x = torch.empty(nin, dtype=torch.float32, device='cuda').uniform_(-1, 1)
     y = torch.empty(nout, dtype=torch.float32, device='cuda')
@@ -434,7 +435,7 @@ def leg_ragged(bb, torch, stream, hbm_peak, steps, warmup):
     info = r.info()
     sptr = stream.cuda_stream
     forms = {}
-    for name, form in (('persistent', r.PERSISTENT), ('grid', r.GRID)):
+    for name, form in (('persistent', r.PERSISTENT), ('grid', r.GRID), ('classes', r.CLASSES)):
         r.set_launch_form(form)
         for _ in range(warmup):
             r.execute(sptr, use_graph=True)
@@ -442,12 +443,13 @@ def leg_ragged(bb, torch, stream, hbm_peak, steps, warmup):
         gbs = info.bytes_moved / ms / 1e6
         forms[name] = {'value': round(gbs, 1), 'frac_of_hbm': round(gbs / hbm_peak, 3),
                        'ms_per_batch': round(ms, 3),
-                       'ctas': int(info.grid) if form == r.PERSISTENT else int(info.num_units)}
+                       'ctas': int(info.grid) if form == r.PERSISTENT else int(info.num_units),
+                       'launches': 1 if form != r.CLASSES else 'one kernel node per tile function'}
     best = max(forms, key=lambda k: forms[k]['value'])
     return {'value': forms[best]['value'], 'unit': 'GB/s', 'form': best,
             'frac_of_hbm': forms[best]['frac_of_hbm'], 'forms': forms,
             'bytes_moved': int(info.bytes_moved), 'units': int(info.num_units),
-            'launches_per_batch': 1}
+            'launches_per_batch': forms[best]['launches']}
 
 
 def leg_spectral(bb, torch, stream, steps, warmup):

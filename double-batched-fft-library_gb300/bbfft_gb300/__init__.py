@@ -359,14 +359,15 @@ class Ragged:
         _check(lib().bbfft_ragged_create(arr, len(items), ctypes.byref(h)))
         self.handle = h
 
-    PERSISTENT, GRID = 0, 1
+    PERSISTENT, GRID, CLASSES = 0, 1, 2
 
     def execute(self, stream=None, use_graph=False):
         _check(lib().bbfft_ragged_execute(self.handle, _stream_ptr(stream), int(bool(use_graph))))
 
     def set_launch_form(self, form):
-        """Ragged.PERSISTENT (CTAs take tiles from a counter) or Ragged.GRID (one CTA per
-        tile); include/bbfft_gb300.h: bbfft_ragged_set_launch_form."""
+        """Ragged.PERSISTENT (CTAs take tiles from a counter), Ragged.GRID (one CTA per
+        tile) or Ragged.CLASSES (one kernel per class of tiles with the same tile
+        function); include/bbfft_gb300.h: bbfft_ragged_set_launch_form."""
         _check(lib().bbfft_ragged_set_launch_form(self.handle, int(form)))
 
     def info(self):

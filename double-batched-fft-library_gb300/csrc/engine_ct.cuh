@@ -454,4 +454,20 @@ __device__ __forceinline__ void fft_tile_ct_ragged(const fft_params &p, long lon
     ct_run<Ctx, R, NC, TT, V, 0, sizeof...(Ps), 1, Ps...>(c, j);
 }
 
+// Ragged batches, one CTA per unit: stage the unit's parameters (item un.x, tile un.y)
+// in shared memory.
+__device__ __forceinline__ int2 stage_unit_params(const ragged_item_dev *__restrict__ items,
+                                                  const int2 *__restrict__ units,
+                                                  fft_params &s_p) {
+    constexpr int NW = static_cast<int>(sizeof(fft_params) / sizeof(int));
+    static_assert(NW <= 256, "parameter block larger than the block");
+    const int2 un = units[blockIdx.x];
+    if (static_cast<int>(threadIdx.x) < NW) {
+        reinterpret_cast<int *>(&s_p)[threadIdx.x] =
+            __ldg(reinterpret_cast<const int *>(&items[un.x].p) + threadIdx.x);
+    }
+    __syncthreads();
+    return un;
+}
+
 } // namespace gbfft

@@ -155,10 +155,20 @@ def ragged_units(outdir):
                '#include "engine_ct.cuh"', '#include "kernels.hpp"', '', 'namespace gbfft {', '']
         for i in sorted(idx):
             prec, kind, nc, T, rad, V = ents[i]
+            targs = 'float, %d, %d, %d, %d, %s' % (kind, nc, T, V, ', '.join(map(str, rad)))
             src += ['__device__ __noinline__ void ragged_ct_%d(const fft_params &p, long long tile) {' % i,
-                    '    fft_tile_ct_ragged<float, %d, %d, %d, %d, %s>(p, tile);' % (kind, nc, T, V, ', '.join(map(str, rad))),
+                    '    fft_tile_ct_ragged<%s>(p, tile);' % targs,
+                    '}', '',
+                    '__global__ void __launch_bounds__(256, 2) ragged_class_ct_%d(const ragged_item_dev *__restrict__ items,' % i,
+                    '                                                        const int2 *__restrict__ units) {',
+                    '    __shared__ __align__(16) fft_params s_p;',
+                    '    const int2 un = stage_unit_params(items, units, s_p);',
+                    '    fft_tile_ct_ragged<%s>(s_p, un.y);' % targs,
                     '}', '']
-        src += ['} // namespace gbfft', '']
+        src += ['const void *ragged_class_kernel_%d(int vid) {' % g, '    switch (vid) {']
+        for i in sorted(idx):
+            src += ['    case %d:' % i, '        return reinterpret_cast<const void *>(&ragged_class_ct_%d);' % i]
+        src += ['    default:', '        return nullptr;', '    }', '}', '', '} // namespace gbfft', '']
         fn = os.path.join(outdir, 'ragged_ct_%d.cu' % g)
         write(fn, '\n'.join(src))
         units.append(fn)
@@ -170,7 +180,14 @@ def ragged_units(outdir):
         inc += ['    case %d:' % i, '        ragged_ct_%d(p, tile);' % i, '        break;']
     inc += ['    }', '}', '']
     write(os.path.join(outdir, 'ragged_ct_dispatch.inc'), '\n'.join(inc))
-    host = ['extern const ct_entry ragged_ct_table[] = {']
+    host = ['const void *ragged_class_kernel_%d(int vid);' % g for g in range(RAGGED_FILES)]
+    host += ['', '// kernel of one class of a ragged batch (grid over the class\'s units), by table index',
+             'const void *ragged_class_kernel(int vid) {',
+             '    const void *f = nullptr;']
+    for g in range(RAGGED_FILES):
+        host += ['    if (!f) {', '        f = ragged_class_kernel_%d(vid);' % g, '    }']
+    host += ['    return f;', '}', '']
+    host += ['extern const ct_entry ragged_ct_table[] = {']
     for prec, kind, nc, T, rad, V in ents:
         host.append('    {%d, %d, %d, %d, %d, %d, {%s}, nullptr},' % (prec, kind, nc, T, V, len(rad), ', '.join(map(str, rad))))
     host += ['};', 'static const int kRaggedSize = %d;' % len(ents), '',

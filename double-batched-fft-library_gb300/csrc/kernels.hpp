@@ -32,5 +32,8 @@ int tc_tile_transforms(int nc);
 
 // persistent kernel of ragged batches (ragged.cu)
 const void *ragged_kernel_ptr(int prec, bool persistent);
+// class form of ragged batches: kernel(items, units) over the units of one class
+const void *ragged_class_kernel(int vid);
+const void *ragged_class_runtime_kernel(int prec, int kind);
 
 } // namespace gbfft

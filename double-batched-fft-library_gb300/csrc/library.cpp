@@ -1493,6 +1493,15 @@ struct bbfft_ragged_s {
     const void *func = nullptr;      // persistent kernel
     const void *grid_func = nullptr; // one CTA per unit
     int form = BBFFT_RAGGED_PERSISTENT;
+    // class form: one kernel per class of units (same tile function), independent graph nodes
+    struct unit_class {
+        const void *func;
+        int offset, count; // units class_units[offset, offset + count)
+        unsigned block;
+        std::size_t smem;
+    };
+    std::vector<unit_class> classes;
+    std::unique_ptr<gbfft::device_buffer> class_units;
     uint64_t bytes = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -1582,6 +1591,43 @@ static void make_ragged(bbfft_ragged_item const *items, std::size_t n, bbfft_rag
     }
     std::stable_sort(units.begin(), units.end(),
                      [](auto const &a, auto const &b) { return a.first > b.first; });
+    // class form: units grouped by tile function, LPT order kept inside a class
+    {
+        std::map<int, std::vector<int>> by_class; // key: vid, or -1 - (prec * 8 + kind)
+        for (std::size_t u = 0; u < units.size(); ++u) {
+            int i = units[u].second.first;
+            int key = dev[i].vid >= 0 ? dev[i].vid : -1 - (r.prec * 8 + dev[i].kind);
+            by_class[key].push_back(static_cast<int>(u));
+        }
+        std::vector<int> cflat;
+        for (auto const &kv : by_class) {
+            bbfft_ragged_s::unit_class c{};
+            c.func = kv.first >= 0 ? ragged_class_kernel(kv.first)
+                                   : ragged_class_runtime_kernel(r.prec, dev[units[kv.second[0]].second.first].kind);
+            if (!c.func) {
+                throw status_error(BBFFT_INTERNAL_ERROR, "ragged class kernel not found");
+            }
+            c.offset = static_cast<int>(cflat.size() / 2);
+            c.count = static_cast<int>(kv.second.size());
+            c.block = 32;
+            c.smem = 0;
+            for (int u : kv.second) {
+                int i = units[u].second.first;
+                pass const &ps = r.passes[i];
+                c.block = std::max(c.block, (ps.block + 31) / 32 * 32);
+                c.smem = std::max(c.smem, ps.smem);
+                cflat.push_back(units[u].second.first);
+                cflat.push_back(units[u].second.second);
+            }
+            if (c.smem > 48 * 1024) {
+                allow_max_smem(c.func, r.device);
+            }
+            r.classes.push_back(c);
+        }
+        r.class_units = std::make_unique<device_buffer>(cflat.size() * sizeof(int));
+        GB_CUDA(cudaMemcpy(r.class_units->ptr, cflat.data(), cflat.size() * sizeof(int),
+                           cudaMemcpyHostToDevice));
+    }
     std::vector<int> flat(2 * units.size());
     for (std::size_t u = 0; u < units.size(); ++u) {
         flat[2 * u] = units[u].second.first;
@@ -1628,6 +1674,15 @@ static void launch_ragged(bbfft_ragged_s &r, cudaStream_t stream) {
     if (r.form == BBFFT_RAGGED_GRID) {
         GB_CUDA(cudaLaunchKernel(r.grid_func, dim3(static_cast<unsigned>(std::max(1, n))),
                                  dim3(r.block), args, r.smem, stream));
+        return;
+    }
+    if (r.form == BBFFT_RAGGED_CLASSES) {
+        for (auto const &c : r.classes) {
+            const void *cu = static_cast<const int2 *>(r.class_units->ptr) + c.offset;
+            void *cargs[] = {&items, &cu};
+            GB_CUDA(cudaLaunchKernel(c.func, dim3(static_cast<unsigned>(c.count)), dim3(c.block),
+                                     cargs, c.smem, stream));
+        }
         return;
     }
     GB_CUDA(cudaMemsetAsync(r.counter->ptr, 0, sizeof(unsigned), stream));
@@ -1970,6 +2025,26 @@ int bbfft_ragged_execute(bbfft_ragged_t ragged, cudaStream_t stream, int use_gra
             gbfft::launch_ragged(*ragged, stream);
             return;
         }
+        if (!ragged->exec && ragged->form == BBFFT_RAGGED_CLASSES) {
+            // one kernel node per class, no edges: the classes may run concurrently
+            GB_CUDA(cudaGraphCreate(&ragged->graph, 0));
+            const void *items = ragged->items->ptr;
+            std::vector<const void *> cus(ragged->classes.size());
+            for (std::size_t c = 0; c < ragged->classes.size(); ++c) {
+                auto const &uc = ragged->classes[c];
+                cus[c] = static_cast<const int2 *>(ragged->class_units->ptr) + uc.offset;
+                void *cargs[] = {&items, &cus[c]};
+                cudaKernelNodeParams kp = {};
+                kp.func = const_cast<void *>(uc.func);
+                kp.gridDim = dim3(static_cast<unsigned>(uc.count));
+                kp.blockDim = dim3(uc.block);
+                kp.sharedMemBytes = static_cast<unsigned>(uc.smem);
+                kp.kernelParams = cargs;
+                cudaGraphNode_t node;
+                GB_CUDA(cudaGraphAddKernelNode(&node, ragged->graph, nullptr, 0, &kp));
+            }
+            GB_CUDA(cudaGraphInstantiate(&ragged->exec, ragged->graph, 0));
+        }
         if (!ragged->exec) {
             cudaStream_t cs;
             GB_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
@@ -2001,7 +2076,8 @@ int bbfft_ragged_execute(bbfft_ragged_t ragged, cudaStream_t stream, int use_gra
 
 int bbfft_ragged_set_launch_form(bbfft_ragged_t ragged, int form) {
     return guarded([&] {
-        if (!ragged || (form != BBFFT_RAGGED_PERSISTENT && form != BBFFT_RAGGED_GRID)) {
+        if (!ragged || (form != BBFFT_RAGGED_PERSISTENT && form != BBFFT_RAGGED_GRID &&
+                        form != BBFFT_RAGGED_CLASSES)) {
             throw status_error(BBFFT_INVALID_ARGUMENT, "null ragged batch or unknown launch form");
         }
         if (form != ragged->form) {

@@ -94,6 +94,33 @@ __global__ void __launch_bounds__(256, 2) ragged_grid_kernel(const ragged_item_d
     }
 }
 
+// Class form: one kernel per class of units; this one runs the classes without a
+// compile-time-size tile function.
+template <class R, int Kind>
+__global__ void __launch_bounds__(256, 2) ragged_class_rt(const ragged_item_dev *__restrict__ items,
+                                                       const int2 *__restrict__ units) {
+    __shared__ __align__(16) fft_params s_p;
+    const int2 un = stage_unit_params(items, units, s_p);
+    fft_tile_at<R, Kind, default_io>(s_p, un.y);
+}
+
+const void *ragged_class_runtime_kernel(int prec, int kind) {
+#define GBFFT_RT_CASE(K)                                                                         \
+    case K:                                                                                      \
+        return prec == 4 ? reinterpret_cast<const void *>(&ragged_class_rt<float, K>)            \
+                         : reinterpret_cast<const void *>(&ragged_class_rt<double, K>);
+    switch (kind) {
+        GBFFT_RT_CASE(kind_c2c)
+        GBFFT_RT_CASE(kind_r2c_half)
+        GBFFT_RT_CASE(kind_r2c_full)
+        GBFFT_RT_CASE(kind_c2r_half)
+        GBFFT_RT_CASE(kind_c2r_full)
+    default:
+        return nullptr;
+    }
+#undef GBFFT_RT_CASE
+}
+
 const void *ragged_kernel_ptr(int prec, bool persistent) {
     if (persistent) {
         return prec == 4 ? reinterpret_cast<const void *>(&ragged_kernel<float>)

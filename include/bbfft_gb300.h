@@ -243,8 +243,12 @@ BBFFT_GB300_API int bbfft_ragged_execute(bbfft_ragged_t ragged, cudaStream_t str
                                          int use_graph);
 #define BBFFT_RAGGED_PERSISTENT 0
 #define BBFFT_RAGGED_GRID 1
-/* Selects the launch form of bbfft_ragged_execute (BBFFT_RAGGED_PERSISTENT or
- * BBFFT_RAGGED_GRID); drops a graph captured for the other form. */
+#define BBFFT_RAGGED_CLASSES 2
+/* Selects the launch form of bbfft_ragged_execute: BBFFT_RAGGED_PERSISTENT or
+ * BBFFT_RAGGED_GRID (one launch), or BBFFT_RAGGED_CLASSES (one kernel per class of
+ * tiles with the same tile function, each sized for that class; as a graph the classes
+ * are independent nodes that may run concurrently).  Drops a graph made for another
+ * form. */
 BBFFT_GB300_API int bbfft_ragged_set_launch_form(bbfft_ragged_t ragged, int form);
 BBFFT_GB300_API int bbfft_ragged_get_info(bbfft_ragged_t ragged, bbfft_ragged_info *info);
 BBFFT_GB300_API int bbfft_ragged_destroy(bbfft_ragged_t ragged);

@@ -51,7 +51,7 @@ def check_items(bb, po, specs, x, y, idx):
     return worst
 
 
-@pytest.mark.parametrize('form', [0, 1])
+@pytest.mark.parametrize('form', [0, 1, 2])
 @pytest.mark.parametrize('use_graph', [False, True])
 def test_ragged_small_batch(bb, po, torch_cuda, use_graph, form):
     torch = torch_cuda
@@ -79,12 +79,14 @@ def test_ragged_benchmark_batch_graph_replay(bb, po, torch_cuda):
     r.execute(s, use_graph=True)
     torch.cuda.synchronize()
     assert torch.equal(first, y)
-    # the grid form (one CTA per tile) computes the same tiles with the same code
-    y.zero_()
-    r.set_launch_form(r.GRID)
-    r.execute(s, use_graph=True)
-    torch.cuda.synchronize()
-    assert torch.equal(first, y)
+    # the grid form (one CTA per tile) and the class form (one kernel per tile function)
+    # compute the same tiles with the same code
+    for form in (r.GRID, r.CLASSES):
+        y.zero_()
+        r.set_launch_form(form)
+        r.execute(s, use_graph=True)
+        torch.cuda.synchronize()
+        assert torch.equal(first, y), form
     rng = np.random.default_rng(5)
     check_items(bb, po, specs, x, y, rng.choice(len(specs), 400, replace=False))
 
