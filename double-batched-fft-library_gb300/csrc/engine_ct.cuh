@@ -460,11 +460,10 @@ __device__ __forceinline__ int2 stage_unit_params(const ragged_item_dev *__restr
                                                   const int2 *__restrict__ units,
                                                   fft_params &s_p) {
     constexpr int NW = static_cast<int>(sizeof(fft_params) / sizeof(int));
-    static_assert(NW <= 256, "parameter block larger than the block");
     const int2 un = units[blockIdx.x];
-    if (static_cast<int>(threadIdx.x) < NW) {
-        reinterpret_cast<int *>(&s_p)[threadIdx.x] =
-            __ldg(reinterpret_cast<const int *>(&items[un.x].p) + threadIdx.x);
+    // the block may have fewer threads than the parameter block has words
+    for (int i = threadIdx.x; i < NW; i += blockDim.x) {
+        reinterpret_cast<int *>(&s_p)[i] = __ldg(reinterpret_cast<const int *>(&items[un.x].p) + i);
     }
     __syncthreads();
     return un;
