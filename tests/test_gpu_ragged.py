@@ -79,14 +79,19 @@ def test_ragged_benchmark_batch_graph_replay(bb, po, torch_cuda):
     r.execute(s, use_graph=True)
     torch.cuda.synchronize()
     assert torch.equal(first, y)
-    # the grid form (one CTA per tile) and the class form (one kernel per tile function)
-    # compute the same tiles with the same code
-    for form in (r.GRID, r.CLASSES):
-        y.zero_()
-        r.set_launch_form(form)
-        r.execute(s, use_graph=True)
-        torch.cuda.synchronize()
-        assert torch.equal(first, y), form
+    # the grid form (one CTA per tile) runs the same compiled tile functions: same bits
+    y.zero_()
+    r.set_launch_form(r.GRID)
+    r.execute(s, use_graph=True)
+    torch.cuda.synchronize()
+    assert torch.equal(first, y)
+    # the class form compiles each tile function into its own kernel (the compiler may
+    # contract multiply-adds differently): equal to rounding
+    y.zero_()
+    r.set_launch_form(r.CLASSES)
+    r.execute(s, use_graph=True)
+    torch.cuda.synchronize()
+    assert float(torch.linalg.vector_norm(y - first) / torch.linalg.vector_norm(first)) <= 1e-6
     rng = np.random.default_rng(5)
     check_items(bb, po, specs, x, y, rng.choice(len(specs), 400, replace=False))
 
