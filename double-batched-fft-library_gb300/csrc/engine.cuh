@@ -254,10 +254,10 @@ __device__ __forceinline__ void run_stage(const transform_ctx<R, Kind, IO> &c, i
 //   X_k = x_0 + sum_j cos(2 pi jk/P) s_j - i sum_j sin(2 pi jk/P) d_j,  X_{P-k} likewise.
 // O(P) work per output.
 //
-// P <= gen_table_max_p: a thread computes whole butterflies, G output pairs per sweep over
-// the input pairs, and the coefficients come from a k-major table w_P^{-(jk mod P)} in
-// shared memory (rows padded to a multiple of G with zeros).  Every lane of a warp reads
-// the same coefficient at the same time (one broadcast load per four FMAs).
+// P <= gen_table_max_p: a task computes G output pairs of one butterfly in one sweep over
+// the input pairs, with the coefficients from a k-major table w_P^{-(jk mod P)} in shared
+// memory (rows padded to a multiple of G with zeros); lanes working on the same group of
+// outputs read the same coefficient (one broadcast load per four FMAs).
 // Larger P: tasks of G output pairs over the threads, coefficients from the w_P table.
 __device__ __forceinline__ int gen_table_rows(int P) {
     return ((P - 1) / 2 + gen_group - 1) / gen_group * gen_group;
@@ -313,44 +313,47 @@ __device__ __forceinline__ void run_stage_generic(const transform_ctx<R, Kind, I
     };
     constexpr int G = gen_group;
     if (table) {
-        for (int b = j; b < nb; b += T) {
+        // task = (group of G output pairs, butterfly), group-major so that the lanes of a
+        // warp mostly share a group and read the same coefficients
+        const int tpb = gen_table_rows(P) / G;
+        for (int task = j; task < nb * tpb; task += T) {
+            const int b = task % nb;
+            const int k0 = 1 + (task / nb) * G;
             const int o = b + (b / Ns) * Ns * (P - 1);
             const C x0 = c.sm[c.sidx(src_buf, b)];
-            for (int k0 = 1; k0 <= H; k0 += G) {
-                const C *w = wtab + (k0 - 1) * H;
-                C acc[G], dd[G];
+            const C *w = wtab + (k0 - 1) * H;
+            C acc[G], dd[G];
 #pragma unroll
-                for (int g = 0; g < G; ++g) {
-                    acc[g] = x0;
-                    dd[g] = mk<R>(R(0), R(0));
-                }
-                C sum = x0;
+            for (int g = 0; g < G; ++g) {
+                acc[g] = x0;
+                dd[g] = mk<R>(R(0), R(0));
+            }
+            C sum = x0;
 #pragma unroll 2
-                for (int jj = 1; jj <= H; ++jj) {
-                    const C xa = c.sm[c.sidx(src_buf, b + jj * nb)];
-                    const C xb = c.sm[c.sidx(src_buf, b + (P - jj) * nb)];
-                    const C sj = cadd(xa, xb);
-                    const C dj = csub(xa, xb);
-                    sum = cadd(sum, sj);
-#pragma unroll
-                    for (int g = 0; g < G; ++g) {
-                        const C cw = w[g * H + jj - 1]; // (cos, -sin)(2 pi jj k / P)
-                        acc[g].x += cw.x * sj.x;
-                        acc[g].y += cw.x * sj.y;
-                        dd[g].x += cw.y * dj.x;
-                        dd[g].y += cw.y * dj.y;
-                    }
-                }
-                if (k0 == 1) {
-                    put(o, 0, sum);
-                }
+            for (int jj = 1; jj <= H; ++jj) {
+                const C xa = c.sm[c.sidx(src_buf, b + jj * nb)];
+                const C xb = c.sm[c.sidx(src_buf, b + (P - jj) * nb)];
+                const C sj = cadd(xa, xb);
+                const C dj = csub(xa, xb);
+                sum = cadd(sum, sj);
 #pragma unroll
                 for (int g = 0; g < G; ++g) {
-                    const int k = k0 + g;
-                    if (k <= H) {
-                        put(o, k, mk<R>(acc[g].x - dd[g].y, acc[g].y + dd[g].x));
-                        put(o, P - k, mk<R>(acc[g].x + dd[g].y, acc[g].y - dd[g].x));
-                    }
+                    const C cw = w[g * H + jj - 1]; // (cos, -sin)(2 pi jj k / P)
+                    acc[g].x += cw.x * sj.x;
+                    acc[g].y += cw.x * sj.y;
+                    dd[g].x += cw.y * dj.x;
+                    dd[g].y += cw.y * dj.y;
+                }
+            }
+            if (k0 == 1) {
+                put(o, 0, sum);
+            }
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                const int k = k0 + g;
+                if (k <= H) {
+                    put(o, k, mk<R>(acc[g].x - dd[g].y, acc[g].y + dd[g].x));
+                    put(o, P - k, mk<R>(acc[g].x + dd[g].y, acc[g].y - dd[g].x));
                 }
             }
         }

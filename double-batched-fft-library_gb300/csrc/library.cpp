@@ -285,7 +285,7 @@ std::vector<char> nvrtc_compile(std::string const &source, std::string const &na
 
 static bool unrolled(int P) { return P == 1 || (P >= 2 && P <= 13) || P == 16; }
 // Generic (non-unrolled) odd radix with the coefficient table of run_stage_generic
-// (engine.cuh): one thread per butterfly.
+// (engine.cuh): one thread per group of gen_group output pairs of a butterfly.
 static bool table_generic(int P) { return !unrolled(P) && P % 2 == 1 && P <= gen_table_max_p; }
 // shared-memory elements the generic stage of radix P needs after the data buffers
 static int gen_shared_elems(int P) {
@@ -875,7 +875,8 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     if (pu == 1) {
         T = std::min(Nc, 64);
     }
-    // with a table-driven generic stage: one thread per butterfly of the largest one
+    // with a table-driven generic stage: one thread per task (a group of gen_group output
+    // pairs of one butterfly) of the largest one
     int ptg = 0;
     for (int r : rad) {
         if (table_generic(r)) {
@@ -883,7 +884,8 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         }
     }
     if (ptg > 0 && q.T <= 0) {
-        T = Nc / ptg;
+        int H = (ptg - 1) / 2;
+        T = Nc / ptg * ((H + gen_group - 1) / gen_group);
     }
     T = std::min(T, 512);
 
