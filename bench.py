@@ -398,9 +398,24 @@ def leg_c2c_cfg1(bb, torch, stream, hbm_peak, steps, warmup):
         one()
     ms = event_time(torch, stream, one, max(steps, 4) * nb)
     b = 2 * M * N * K * 8
-    return {'value': round(b / ms / 1e6, 1), 'unit': 'GB/s',
-            'frac_of_hbm': round(b / ms / 1e6 / hbm_peak, 3),
-            'us_per_launch': round(ms * 1e3, 2), 'l2': '24 rotating buffer pairs, 384 MiB'}
+    # the same 24 launches captured once in a CUDA graph and replayed (no per-launch host
+    # work between the kernels)
+    g = torch.cuda.CUDAGraph()
+    cs = torch.cuda.Stream()
+    cs.wait_stream(stream)
+    with torch.cuda.graph(g, stream=cs):
+        for i in range(nb):
+            plan.execute_on(xs[i].data_ptr(), ys[i].data_ptr(), cs.cuda_stream)
+    stream.wait_stream(cs)
+    for _ in range(warmup):
+        g.replay()
+    msg = event_time(torch, torch.cuda.current_stream(), g.replay, max(steps, 4)) / nb
+    best = min(ms, msg)
+    return {'value': round(b / best / 1e6, 1), 'unit': 'GB/s',
+            'frac_of_hbm': round(b / best / 1e6 / hbm_peak, 3),
+            'us_per_launch_stream': round(ms * 1e3, 2), 'us_per_launch_graph': round(msg * 1e3, 2),
+            'gbs_stream': round(b / ms / 1e6, 1), 'gbs_graph': round(b / msg / 1e6, 1),
+            'l2': '24 rotating buffer pairs, 384 MiB'}
 
 
 def ragged_specs(bb, n=10000, seed=4):

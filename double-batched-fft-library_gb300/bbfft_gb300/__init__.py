@@ -82,6 +82,7 @@ class PlanInfo(ctypes.Structure):
         ('workspace_bytes', ctypes.c_size_t),
         ('vector_width', ctypes.c_uint32),
         ('specialized', ctypes.c_uint32),
+        ('min_blocks', ctypes.c_uint32),
     ]
 
 
@@ -142,7 +143,8 @@ _SIGNATURES = {
     'bbfft_plan_create_tuned': (ctypes.c_int, [ctypes.POINTER(Configuration), _vp,
                                                ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint32,
                                                ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
-                                               ctypes.c_uint32, ctypes.POINTER(_vp)]),
+                                               ctypes.c_uint32, ctypes.c_uint32,
+                                               ctypes.POINTER(_vp)]),
     'bbfft_plan_execute': (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_uint32, ctypes.POINTER(_vp), _vp]),
     'bbfft_plan_execute_on': (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     'bbfft_plan_retain': (ctypes.c_int, [_vp]),
@@ -308,10 +310,12 @@ class Plan:
         L = lib()
         s = _stream_ptr(stream)
         if tuning is not None:
-            rad, T, V, mb, kb = tuning
+            rad, T, V, mb, kb = tuning[:5]
+            occ = tuning[5] if len(tuning) > 5 else 0
             arr = (ctypes.c_uint32 * max(1, len(rad)))(*rad) if rad else None
             _check(L.bbfft_plan_create_tuned(ctypes.byref(cfg), s, arr, len(rad) if rad else 0,
-                                             T or 0, V or 0, mb or 0, kb or 0, ctypes.byref(h)))
+                                             T or 0, V or 0, mb or 0, kb or 0, occ or 0,
+                                             ctypes.byref(h)))
         else:
             fn = L.bbfft_plan_create_adjoint if adjoint else L.bbfft_plan_create
             _check(fn(ctypes.byref(cfg), s, cache.handle if cache else None, ctypes.byref(h)))

@@ -4,7 +4,8 @@ For a 1d configuration the tuner times candidate blockings of the plan -- transf
 thread along M (V), the M- and K-extent of a CTA tile (Mb, Kb) -- with CUDA events on
 device-resident data and records the fastest in a tuning table.  bbfft_plan_create
 consults the table (one line per precision, kernel kind, N and M:
-``<prec> <kind> <N> <M> <V> <Mb> <Kb>``).  The radices and threads per transform stay
+``<prec> <kind> <N> <M> <V> <Mb> <Kb> <CTAs per SM>``, the last being the resident-CTA
+count the compile-time kernel's registers are sized for).  The radices and threads per transform stay
 those of the library's heuristic, which the compile-time kernels are instantiated for.
 
 Usage (on the GPU):  python -m bbfft_gb300.autotune [--out PATH] [--quick]
@@ -39,15 +40,17 @@ def tune_config(torch, prec, type, N, M, K, reps=4, verbose=False):
     stream = torch.cuda.current_stream()
     results = {}
     mbs = sorted({m for m in (M, 64, 32, 16, 8, 4, 2, 1) if m <= M and m <= 64}, reverse=True)
+    occs = (2, 3) if prec == 4 else (2,)
     for V in (0, 1, 2, 4):
         for Mb in mbs:
             for Kb in (0, 1, 2, 4, 8, 16, 32, 64, 128, 256):
+              for occ in occs:
                 try:
-                    plan = bb.Plan(cfg, stream=stream.cuda_stream, tuning=(None, 0, V, Mb, Kb))
+                    plan = bb.Plan(cfg, stream=stream.cuda_stream, tuning=(None, 0, V, Mb, Kb, occ))
                 except bb.BBFFTError:
                     continue
                 info = plan.info()
-                key = (info.vector_width, info.mb, info.kb)
+                key = (info.vector_width, info.mb, info.kb, info.min_blocks or 2)
                 if key in results:
                     continue
                 for _ in range(2):
@@ -70,9 +73,9 @@ def tune_config(torch, prec, type, N, M, K, reps=4, verbose=False):
     entry = (prec, kind, N, M) + best_key
     if verbose:
         worst = max(r[0] for r in results.values())
-        print('prec %d type %d N %4d M %4d: best V=%d Mb=%d Kb=%d %.1f GB/s (%d candidates, worst %.2fx)'
-              % (prec, type, N, M, best_key[0], best_key[1], best_key[2], gbs, len(results),
-                 worst / results[best_key][0]), flush=True)
+        print('prec %d type %d N %4d M %4d: best V=%d Mb=%d Kb=%d occ=%d %.1f GB/s (%d candidates, '
+              'worst %.2fx)' % (prec, type, N, M, best_key[0], best_key[1], best_key[2], best_key[3],
+                                gbs, len(results), worst / results[best_key][0]), flush=True)
     return entry, gbs
 
 
@@ -99,12 +102,32 @@ def default_configs(quick=False):
     return cfgs
 
 
+def read_table(path):
+    """Entries of an existing table as (prec, kind, N, M, V, Mb, Kb, occ), GB/s."""
+    out = []
+    if not os.path.exists(path):
+        return out
+    for line in open(path):
+        body, _, note = line.partition('#')
+        f = body.split()
+        if len(f) < 7:
+            continue
+        occ = int(f[7]) if len(f) > 7 else 2
+        e = (int(f[0]), f[1], int(f[2]), int(f[3]), int(f[4]), int(f[5]), int(f[6]), occ)
+        try:
+            gbs = float(note.strip())
+        except ValueError:
+            gbs = 0.0
+        out.append((e, gbs))
+    return out
+
+
 def write_table(path, entries):
     os.makedirs(os.path.dirname(path), exist_ok=True)
-    lines = ['# bbfft GB300 tuning table: <prec bytes> <kind> <N> <M> <V> <Mb> <Kb>  # GB/s',
+    lines = ['# bbfft GB300 tuning table: <prec bytes> <kind> <N> <M> <V> <Mb> <Kb> <CTAs per SM>  # GB/s',
              '# written by bbfft_gb300/autotune.py from CUDA-event timings on a GB300']
     for e, gbs in entries:
-        lines.append('%d %s %d %d %d %d %d  # %.1f' % (e + (gbs,)))
+        lines.append('%d %s %d %d %d %d %d %d  # %.1f' % (e + (gbs,)))
     with open(path, 'w') as f:
         f.write('\n'.join(lines) + '\n')
 
@@ -113,13 +136,21 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument('--out', default=DEFAULT_OUT)
     ap.add_argument('--quick', action='store_true')
+    ap.add_argument('--only-n', default='', help='comma-separated N: retune these, keep the rest')
+    ap.add_argument('--prec', type=int, default=0, help='4 or 8: tune one precision only')
     args = ap.parse_args(argv)
     import torch
 
     os.environ['BBFFT_GB300_TUNING'] = 'off'  # candidates are set explicitly
+    only = {int(n) for n in args.only_n.split(',') if n}
+    kept = read_table(args.out) if only else []
     entries = []
     for prec, type, N, M, K in default_configs(args.quick):
+        if (only and N not in only) or (args.prec and prec != args.prec):
+            continue
         entries.append(tune_config(torch, prec, type, N, M, K, verbose=True))
+    fresh = {e[:4] for e, _ in entries}
+    entries = [(e, g) for e, g in kept if e[:4] not in fresh] + entries
     write_table(args.out, entries)
     print('wrote', args.out)
 

@@ -110,7 +110,10 @@ def entries():
                 if any(r not in UNROLLED for r in rad):
                     continue
                 for V in sorted({1, vector_width(prec, rad)}):
-                    out.append((prec, kind, nc, T, rad, V))
+                    # resident CTAs the register allocation is sized for: 2 (up to 128
+                    # registers), and for float also 3 (up to 80), chosen by the autotuner
+                    for minb in ((2, 3) if prec == 4 else (2,)):
+                        out.append((prec, kind, nc, T, rad, V, minb))
     return out
 
 
@@ -189,7 +192,7 @@ def ragged_units(outdir):
     host += ['    return f;', '}', '']
     host += ['extern const ct_entry ragged_ct_table[] = {']
     for prec, kind, nc, T, rad, V in ents:
-        host.append('    {%d, %d, %d, %d, %d, %d, {%s}, nullptr},' % (prec, kind, nc, T, V, len(rad), ', '.join(map(str, rad))))
+        host.append('    {%d, %d, %d, %d, %d, %d, {%s}, nullptr, 2},' % (prec, kind, nc, T, V, len(rad), ', '.join(map(str, rad))))
     host += ['};', 'static const int kRaggedSize = %d;' % len(ents), '',
              'int ragged_ct_lookup(int prec, int kind, int nc, int T, int V, const int *rad, int L) {',
              '    for (int i = 0; i < kRaggedSize; ++i) {',
@@ -214,8 +217,8 @@ def main(outdir):
     os.makedirs(outdir, exist_ok=True)
     ents = entries()
     files = {}
-    for prec, kind, nc, T, rad, V in ents:
-        files.setdefault((prec, kind), []).append((nc, T, rad, V))
+    for prec, kind, nc, T, rad, V, minb in ents:
+        files.setdefault((prec, kind), []).append((nc, T, rad, V, minb))
     index = ['// generated by gen_specializations.py', '#include "kernels.hpp"', '',
              'namespace gbfft {']
     tables = []
@@ -224,14 +227,14 @@ def main(outdir):
         name = 'ct_table_f%d_%s' % (prec * 8, KINDS[kind])
         src = ['// generated by gen_specializations.py: compile-time-size FFT kernels',
                '#include "engine_ct.cuh"', '#include "kernels.hpp"', '', 'namespace gbfft {', '',
-               'template <class R, int Kind, int NC, int TT, int V, int... Ps>',
-               '__global__ void __launch_bounds__(256, 2) fft_kernel_ct(const __grid_constant__ fft_params p) {',
+               'template <class R, int Kind, int NC, int TT, int V, int MINB, int... Ps>',
+               '__global__ void __launch_bounds__(256, MINB) fft_kernel_ct(const __grid_constant__ fft_params p) {',
                '    fft_tile_ct<R, Kind, NC, TT, V, Ps...>(p);', '}', '',
                'extern const ct_entry %s[] = {' % name]
-        for nc, T, rad, V in lst:
+        for nc, T, rad, V, minb in lst:
             rs = ', '.join(map(str, rad))
-            src.append('    {%d, %d, %d, %d, %d, %d, {%s}, reinterpret_cast<const void *>(&fft_kernel_ct<%s, %d, %d, %d, %d, %s>)},'
-                       % (prec, kind, nc, T, V, len(rad), rs, R, kind, nc, T, V, rs))
+            src.append('    {%d, %d, %d, %d, %d, %d, {%s}, reinterpret_cast<const void *>(&fft_kernel_ct<%s, %d, %d, %d, %d, %d, %s>), %d},'
+                       % (prec, kind, nc, T, V, len(rad), rs, R, kind, nc, T, V, minb, rs, minb))
         src += ['};', 'extern const int %s_size = %d;' % (name, len(lst)), '', '} // namespace gbfft', '']
         fn = os.path.join(outdir, 'kernels_ct_f%d_%s.cu' % (prec * 8, KINDS[kind]))
         text = '\n'.join(src)
@@ -244,11 +247,13 @@ def main(outdir):
     index += ['', 'static const ct_entry *const kTables[] = {%s};' % ', '.join(tables),
               'static const int *const kSizes[] = {%s};' % ', '.join('&%s_size' % t for t in tables),
               '',
-              'const ct_entry *ct_lookup(int prec, int kind, int nc, int T, int V, const int *rad, int L) {',
+              'const ct_entry *ct_lookup(int prec, int kind, int nc, int T, int V, const int *rad, int L,',
+              '                          int minb) {',
               '    for (unsigned t = 0; t < sizeof(kTables) / sizeof(kTables[0]); ++t) {',
               '        for (int i = 0; i < *kSizes[t]; ++i) {',
               '            const ct_entry &e = kTables[t][i];',
-              '            if (e.prec != prec || e.kind != kind || e.nc != nc || e.T != T || e.V != V || e.L != L) {',
+              '            if (e.prec != prec || e.kind != kind || e.nc != nc || e.T != T || e.V != V || e.L != L ||',
+              '                e.minb != minb) {',
               '                continue;',
               '            }',
               '            bool same = true;',

@@ -19,8 +19,10 @@ struct ct_entry {
     int L;       // number of stages
     int rad[12]; // radices
     const void *fn;
+    int minb;    // resident CTAs of 256 threads the register allocation is sized for
 };
-const ct_entry *ct_lookup(int prec, int kind, int nc, int T, int V, const int *rad, int L);
+const ct_entry *ct_lookup(int prec, int kind, int nc, int T, int V, const int *rad, int L,
+                          int minb);
 // compile-time-size tiles of the persistent ragged kernel: index into ragged_ct_table or -1
 extern const ct_entry ragged_ct_table[];
 int ragged_ct_lookup(int prec, int kind, int nc, int T, int V, const int *rad, int L);

@@ -389,6 +389,7 @@ struct pass {
     int V = 1;                // transforms per thread along M
     std::shared_ptr<pass> scalar_alt; // V = 1 variant for pointers not aligned to 16 bytes
     int ragged_vid = -1;              // compile-time-size tile of the ragged kernel, or -1
+    int min_blocks = 0;               // register budget of the compile-time kernel (0: none)
     std::string identifier;
     int in_sel = 0;  // 0: user input, 2: temporary
     int out_sel = 1; // 1: user output, 2: temporary
@@ -407,6 +408,7 @@ struct pass_request {
     std::vector<int> radices;
     int T = 0, Mb = 0, Kb = 0;
     int V = 0; // 0: automatic, 1: no vectorisation along M, > 1: requested width
+    int occ = 0; // resident CTAs of the compile-time kernel's register budget (0: automatic)
     bool force_v1 = false;
     bool runtime_only = false; // runtime-size kernel (ragged batches)
     int compute = BBFFT_COMPUTE_NATIVE;
@@ -421,6 +423,7 @@ struct pass_request {
 
 struct tune_entry {
     int V, Mb, Kb;
+    int occ; // resident CTAs the kernel's registers are sized for (2 or 3)
 };
 
 static std::string library_dir() {
@@ -450,11 +453,14 @@ static std::map<std::tuple<int, std::string, int, long long>, tune_entry> const 
                 line = line.substr(0, hash);
             }
             std::istringstream ls(line);
-            int prec, N, V, Mb, Kb;
+            int prec, N, V, Mb, Kb, occ = 2;
             long long M;
             std::string kind;
             if (ls >> prec >> kind >> N >> M >> V >> Mb >> Kb) {
-                table[std::make_tuple(prec, kind, N, M)] = tune_entry{V, Mb, Kb};
+                if (!(ls >> occ) || (occ != 2 && occ != 3)) {
+                    occ = 2; // optional eighth column
+                }
+                table[std::make_tuple(prec, kind, N, M)] = tune_entry{V, Mb, Kb, occ};
             }
         }
     });
@@ -891,15 +897,17 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
 
     long long M = q.M, K = q.K;
     bool has_cb = (q.load_fn && *q.load_fn) || (q.store_fn && *q.store_fn);
-    int reqV = q.V, reqMb = q.Mb, reqKb = q.Kb;
-    if (q.radices.empty() && q.T == 0 && q.V == 0 && q.Mb == 0 && q.Kb == 0 && !q.force_v1 &&
-        !q.runtime_only) {
+    int reqV = q.V, reqMb = q.Mb, reqKb = q.Kb, reqOcc = q.occ;
+    if (q.radices.empty() && q.T == 0 && q.V == 0 && q.Mb == 0 && q.Kb == 0 && q.occ == 0 &&
+        !q.force_v1 && !q.runtime_only) {
         if (auto te = find_tuning(q.prec, ps.kind, N, M)) {
             reqV = te->V;
             reqMb = te->Mb;
             reqKb = te->Kb;
+            reqOcc = te->occ;
         }
     }
+    int const minb = reqOcc == 3 ? 3 : 2;
     // compile-time-size kernel, vectorised over M when the layout allows it
     const ct_entry *ct = nullptr;
     int V = 1;
@@ -911,11 +919,11 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         bool v_ok = !q.force_v1 && vw > 1 && M % vw == 0 && q.is1 % vw == 0 && q.os1 % vw == 0 &&
                     q.is2 % vw == 0 && q.os2 % vw == 0;
         if (v_ok) {
-            ct = ct_lookup(q.prec, ps.kind, Nc, T, vw, rad.data(), L);
+            ct = ct_lookup(q.prec, ps.kind, Nc, T, vw, rad.data(), L, minb);
             V = ct ? vw : 1;
         }
         if (!ct) {
-            ct = ct_lookup(q.prec, ps.kind, Nc, T, 1, rad.data(), L);
+            ct = ct_lookup(q.prec, ps.kind, Nc, T, 1, rad.data(), L, minb);
         }
     }
     // ragged batches: compile-time-size tile functions of the persistent kernel (float, V = 1)
@@ -1055,6 +1063,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     if (!has_cb) {
         ps.func = (ct && ct->fn) ? ct->fn : (q.prec == 4 ? kernel_f32(ps.kind) : kernel_f64(ps.kind));
         ps.specialized = ct != nullptr;
+        ps.min_blocks = ct ? ct->minb : 0;
         ps.ragged_vid = ragged_vid;
         if (V > 1) {
             pass_request q1 = q;
@@ -1141,7 +1150,7 @@ const char *plan_pass_fixed(int prec, int type, int dir, long long M, long long 
     }
     int T = pu == 1 ? std::min(Nc, 64) : std::max(1, Nc / pu);
     T = std::min(T, 512);
-    const ct_entry *ct = ct_lookup(prec, kind, Nc, T, 1, rad, L);
+    const ct_entry *ct = ct_lookup(prec, kind, Nc, T, 1, rad, L, 2);
     int const max_block = ct ? 256 : 512;
     int nbuf = 1;
     for (int s2 = 0; s2 < L && !ct; ++s2) {
@@ -1942,7 +1951,7 @@ int bbfft_plan_create_adjoint(const bbfft_configuration *cfg, cudaStream_t strea
 int bbfft_plan_create_tuned(const bbfft_configuration *cfg, cudaStream_t stream,
                             const uint32_t *radices, uint32_t num_radices,
                             uint32_t threads_per_transform, uint32_t vector_width, uint32_t mb,
-                            uint32_t kb, bbfft_plan_t *plan) {
+                            uint32_t kb, uint32_t min_blocks, bbfft_plan_t *plan) {
     gbfft::pass_request t{};
     if (radices) {
         for (uint32_t i = 0; i < num_radices && radices[i] != 0; ++i) {
@@ -1954,6 +1963,7 @@ int bbfft_plan_create_tuned(const bbfft_configuration *cfg, cudaStream_t stream,
     t.force_v1 = vector_width == 1;
     t.Mb = static_cast<int>(mb);
     t.Kb = static_cast<int>(kb);
+    t.occ = static_cast<int>(min_blocks);
     if (cfg && cfg->dim != 1) {
         gbfft::tl_error = "tuned plans are 1d only";
         return BBFFT_BAD_CONFIGURATION;
@@ -2136,6 +2146,7 @@ int bbfft_plan_get_info(bbfft_plan_t plan, bbfft_plan_info *info) {
         info->workspace_bytes = plan->tmp ? plan->tmp->bytes : 0;
         info->vector_width = static_cast<uint32_t>(ps.V);
         info->specialized = ps.specialized ? 1u : 0u;
+        info->min_blocks = static_cast<uint32_t>(ps.min_blocks);
     });
 }
 

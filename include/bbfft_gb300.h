@@ -194,20 +194,22 @@ typedef struct bbfft_plan_info {
     size_t workspace_bytes; /* device scratch owned by the plan (nd temporaries) */
     uint32_t vector_width;  /* transforms per thread along M (first pass) */
     uint32_t specialized;   /* 1 if the first pass runs a compile-time-size kernel */
+    uint32_t min_blocks;    /* its register budget: resident CTAs of 256 threads (0: none) */
 } bbfft_plan_info;
 BBFFT_GB300_API int bbfft_plan_get_info(bbfft_plan_t plan, bbfft_plan_info *info);
 
 /* Override the automatic blocking of a 1d plan (autotuner hook; no counterpart in the
  * reference).  radices: list whose product is the complex FFT length (NULL / 0 entries =
  * automatic); threads_per_transform, mb, kb: 0 = automatic; vector_width: transforms per
- * thread along M (0 = automatic, 1 = none).  Plans made with bbfft_plan_create consult the
- * tuning table (BBFFT_GB300_TUNING or the package's tuning/gb300.tune) written by the
- * autotuner. */
+ * thread along M (0 = automatic, 1 = none); min_blocks: 2 or 3 resident CTAs of 256
+ * threads that the compile-time kernel's registers are sized for (0 = automatic, float
+ * only for 3).  Plans made with bbfft_plan_create consult the tuning table
+ * (BBFFT_GB300_TUNING or the package's tuning/gb300.tune) written by the autotuner. */
 BBFFT_GB300_API int bbfft_plan_create_tuned(const bbfft_configuration *cfg, cudaStream_t stream,
                                             const uint32_t *radices, uint32_t num_radices,
                                             uint32_t threads_per_transform,
                                             uint32_t vector_width, uint32_t mb, uint32_t kb,
-                                            bbfft_plan_t *plan);
+                                            uint32_t min_blocks, bbfft_plan_t *plan);
 
 /* ---- ragged batches (no counterpart in the reference, which launches one kernel per plan,
  *      src/common/algorithm/small_batch_fft.hpp:111) ---- */
