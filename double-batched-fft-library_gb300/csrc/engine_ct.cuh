@@ -276,9 +276,132 @@ template <class R, int Kind, int NC, int TT, int V, bool MI = false> struct ct_c
     }
 };
 
+// Odd prime radix 17..61 with compile-time roots of unity (shared memory in and out, one
+// transform per thread along M).  A task is one group of G output pairs (k, P-k) of one
+// butterfly; consecutive threads take consecutive butterflies of the same group, so the
+// lanes of a warp mostly run the same group and every coefficient is a literal operand
+// of its FMA.  With s_j = x_j + x_{P-j}, d_j = x_j - x_{P-j} (the reference's pair
+// optimisation, src/base/mixed_radix_fft.cpp:55-126):
+//   X_k = x_0 + sum_j cos(2 pi jk/P) s_j - i sum_j sin(2 pi jk/P) d_j,  X_{P-k} likewise.
+// The stage twiddles are applied in place first; the results stay in registers until
+// every task has read its inputs (the stage runs in place).
+__host__ __device__ constexpr bool ct_big_prime(int P) { return P > 16 && P <= 61 && P % 2 == 1; }
+
+template <int P, int GRP, int G, class Ctx, class R>
+__device__ __forceinline__ void ct_prime_group(const Ctx &c, int b, int nb, cplx<R> *out) {
+    using C = cplx<R>;
+    constexpr int H = (P - 1) / 2;
+    C x0[1];
+    c.sload(b, x0);
+    C acc[G], dd[G];
+    sfor<0, G>([&](auto Q) {
+        acc[Q.value] = x0[0];
+        dd[Q.value] = mk<R>(R(0), R(0));
+    });
+    C sum = x0[0];
+    sfor<1, H + 1>([&](auto J) {
+        constexpr int jj = decltype(J)::value;
+        C xa[1], xb[1];
+        c.sload(b + jj * nb, xa);
+        c.sload(b + (P - jj) * nb, xb);
+        const C sj = cadd(xa[0], xb[0]);
+        const C dj = csub(xa[0], xb[0]);
+        if constexpr (GRP == 0) {
+            sum = cadd(sum, sj);
+        }
+        sfor<0, G>([&](auto Q) {
+            constexpr int k = GRP * G + decltype(Q)::value + 1;
+            if constexpr (k <= H) {
+                constexpr R cr = W<R, P, jj * k>::re; //  cos(2 pi jj k / P)
+                constexpr R ci = W<R, P, jj * k>::im; // -sin(2 pi jj k / P)
+                acc[Q.value].x += cr * sj.x;
+                acc[Q.value].y += cr * sj.y;
+                dd[Q.value].x += ci * dj.x;
+                dd[Q.value].y += ci * dj.y;
+            }
+        });
+    });
+    out[0] = sum;
+    sfor<0, G>([&](auto Q) {
+        out[1 + 2 * Q.value] = mk<R>(acc[Q.value].x - dd[Q.value].y, acc[Q.value].y + dd[Q.value].x);
+        out[2 + 2 * Q.value] = mk<R>(acc[Q.value].x + dd[Q.value].y, acc[Q.value].y - dd[Q.value].x);
+    });
+}
+
+template <int P, int NS, class Ctx, class R, int NC, int TT>
+__device__ __forceinline__ void ct_stage_prime(const Ctx &c, int j) {
+    using C = cplx<R>;
+    constexpr int nb = NC / P;
+    constexpr int H = (P - 1) / 2;
+    constexpr int G = sizeof(R) == 4 ? 8 : 4;
+    constexpr int NG = (H + G - 1) / G;
+    constexpr int NT = nb * NG;
+    constexpr int ITERS = (NT + TT - 1) / TT;
+    constexpr int twstride = (Ctx::half ? 2 * NC : NC) / (NS * P);
+    const bool live = !Ctx::may_idle || c.live;
+    if constexpr (NS > 1) {
+        const C *tw = static_cast<const C *>(c.p.tw);
+        constexpr int IE = (NC + TT - 1) / TT;
+#pragma unroll
+        for (int it = 0; it < IE; ++it) {
+            const int e = j + it * TT;
+            if (live && (NC % TT == 0 || e < NC)) {
+                const int b = e % nb;
+                const int r = e / nb;
+                if (r > 0) {
+                    C v[1];
+                    c.sload(e, v);
+                    v[0] = cmul(v[0], __ldg(tw + r * (b % NS) * twstride));
+                    c.sstore(e, v);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    C out[ITERS][2 * G + 1];
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int t = j + it * TT;
+        if (live && (NT % TT == 0 || t < NT)) {
+            const int grp = t / nb;
+            const int b = t % nb;
+            sfor<0, NG>([&](auto Gi) {
+                if (grp == Gi.value) {
+                    ct_prime_group<P, Gi.value, G, Ctx, R>(c, b, nb, out[it]);
+                }
+            });
+        }
+    }
+    __syncthreads(); // every input is read before the outputs overwrite the buffer
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int t = j + it * TT;
+        if (live && (NT % TT == 0 || t < NT)) {
+            const int grp = t / nb;
+            const int b = t % nb;
+            const int o = b + (b / NS) * NS * (P - 1);
+            if (grp == 0) {
+                c.sstore(o, &out[it][0]);
+            }
+            sfor<0, G>([&](auto Q) {
+                const int k = grp * G + Q.value + 1;
+                if (k <= H) {
+                    c.sstore(o + k * NS, &out[it][1 + 2 * Q.value]);
+                    c.sstore(o + (P - k) * NS, &out[it][2 + 2 * Q.value]);
+                }
+            });
+        }
+    }
+}
+
 // One in-place Stockham stage with compile-time sizes (see engine.cuh for the formulas).
 template <int P, int NS, bool SRC_G, bool DST_G, class Ctx, class R, int NC, int TT, int V>
 __device__ __forceinline__ void ct_stage(const Ctx &c, int j) {
+    if constexpr (ct_big_prime(P)) {
+        static_assert(!SRC_G && !DST_G && V == 1, "prime stages run shared to shared, V = 1");
+        ct_stage_prime<P, NS, Ctx, R, NC, TT>(c, j);
+        return;
+    } else {
     using C = cplx<R>;
     constexpr int nb = NC / P;
     constexpr int ITERS = (nb + TT - 1) / TT;
@@ -338,6 +461,7 @@ __device__ __forceinline__ void ct_stage(const Ctx &c, int j) {
                 }
             });
         }
+    }
     }
 }
 

@@ -73,17 +73,26 @@ def choose_radices(nc):
     return r + big
 
 
-def stage_list(nc, kind):
-    """Radices incl. the copy stages the host adds, and threads per transform."""
+BIG_PRIMES = {17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61}
+
+
+def stage_list(nc, kind, ragged=False):
+    """Radices incl. the copy stages the host adds, and threads per transform (the rules
+    of make_1d_pass in library.cpp; `ragged`: a pass of a ragged batch)."""
     rad = choose_radices(nc)
     if rad[0] not in UNROLLED:
         rad = [1] + rad
     real = kind != 0
     post = kind == 1
+    if ragged and not post and rad[-1] in BIG_PRIMES:
+        rad = rad + [1]
     if real and not post and len(rad) == 1:
         rad = rad + [1]
     pu = max([r for r in rad if r in UNROLLED] + [1])
     T = max(1, nc // pu) if pu > 1 else min(nc, 64)
+    ptg = max([r for r in rad if r in BIG_PRIMES] + [0])
+    if ptg:
+        T = nc // ptg * (((ptg - 1) // 2 + 7) // 8)
     T = min(T, 512)
     return rad, T
 
@@ -126,8 +135,8 @@ def ragged_entries():
     out = []
     for kind, ncs in ((0, range(16, 513, 8)), (1, range(8, 257, 4))):
         for nc in ncs:
-            rad, T = stage_list(nc, kind)
-            if any(r not in UNROLLED for r in rad):
+            rad, T = stage_list(nc, kind, ragged=True)
+            if any(r not in UNROLLED and r not in BIG_PRIMES for r in rad):
                 continue
             out.append((4, kind, nc, T, rad, 1))
     return out
@@ -144,7 +153,7 @@ def ragged_units(outdir):
     ragged_ct_dispatch.inc (declarations and the switch, included by ragged.cu) and the
     host table lines for ct_index.cpp."""
     ents = ragged_entries()
-    cost = lambda e: e[2] * len(e[4])
+    cost = lambda e: e[2] * len(e[4]) + sum(r * r * 8 for r in e[4] if r in BIG_PRIMES)
     order = sorted(range(len(ents)), key=lambda i: -cost(ents[i]))
     groups = [[] for _ in range(RAGGED_FILES)]
     load = [0] * RAGGED_FILES

@@ -862,6 +862,11 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     if (!unrolled(rad.front())) {
         rad.insert(rad.begin(), 1);
     }
+    // ragged batches: the compile-time prime stages write shared memory only, so a prime
+    // last stage is followed by a copy stage (the same radices for the runtime engine)
+    if (q.runtime_only && !post && table_generic(rad.back())) {
+        rad.push_back(1);
+    }
     // real transforms must finish all global reads of a tile before the first global write
     // (in-place safety): with a single global->global stage, add a shared round trip
     if (is_real && !post && rad.size() == 1) {
