@@ -976,7 +976,8 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     for (int r : rad) {
         pgen = std::max(pgen, gen_shared_elems(r));
     }
-    std::size_t const gen_extra = static_cast<std::size_t>(pgen) * celem;
+    // (compile-time kernels keep their prime coefficients in the code)
+    std::size_t const gen_extra = ct ? 0 : static_cast<std::size_t>(pgen) * celem;
     // shared padding i -> i + (i >> shift) * add adds at most a quarter (choose_padding)
     auto buf_elems = [&](int kb, int mb) {
         long long last = static_cast<long long>(kb) * Nc * mb - 1;
