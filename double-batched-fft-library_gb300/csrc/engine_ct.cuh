@@ -519,11 +519,73 @@ __device__ __forceinline__ void ct_r2c_post(const Ctx &c, int j) {
     }
 }
 
+// c2r (even N) pre-process into the shared buffer, V transforms per thread.  Z[n] and
+// Z[NC-n] need the same two inputs X[n], X[NC-n] and twiddles w_N^{-n}, w_N^{-(NC-n)} =
+// -conj(w_N^{-n}), so one thread forms both (reference formula: sbfft_gen.cpp:209-246):
+//   Z[n] = (x1 + x2) + (x1 - x2) i conj(w_N^{-n}),  x1 = X[n], x2 = conj X[NC-n]
+// (imag X[0] ignored), stored conjugated for the forward engine.
+template <class Ctx, class R, int NC, int TT, int V>
+__device__ __forceinline__ void ct_c2r_pre(const Ctx &c, int j) {
+    using C = cplx<R>;
+    constexpr int cnt = NC / 2 + 1;
+    constexpr int ITERS = (cnt + TT - 1) / TT;
+    const C *X = static_cast<const C *>(c.p.in) + c.ib;
+    const C *tw = static_cast<const C *>(c.p.tw);
+    const bool adj = c.p.flags & flag_adj_r2c;
+    auto z_of = [&](C a1, C a2, C iw, int k1, int k2, bool zero_im) {
+        if (zero_im) {
+            a1.y = R(0);
+        }
+        if (adj) {
+            a1 = c.adj_r2c_weight(a1, k1);
+            a2 = c.adj_r2c_weight(a2, k2);
+        }
+        a2.y = -a2.y;
+        C z = cadd(cadd(a1, a2), cmul(csub(a1, a2), iw));
+        z.y = -z.y;
+        return z;
+    };
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int n = j + it * TT;
+        if ((cnt % TT == 0 || n < cnt) && (!Ctx::may_idle || c.live)) {
+            const int m = NC - n;
+            C x1[V], x2[V], zn[V], zm[V];
+            if (c.active) {
+                ldv<V>(X + n * c.p.is1, x1);
+                ldv<V>(X + m * c.p.is1, x2);
+            } else {
+                sfor<0, V>([&](auto U) {
+                    x1[U.value] = mk<R>(R(0), R(0));
+                    x2[U.value] = mk<R>(R(0), R(0));
+                });
+            }
+            const C w = __ldg(tw + n);
+            const C iw = mk<R>(w.y, w.x);  // i conj(w_N^{-n})
+            const C iwm = mk<R>(w.y, -w.x); // i conj(w_N^{-(NC-n)}), w_N^{-(NC-n)} = -conj(w)
+            sfor<0, V>([&](auto U) {
+                zn[U.value] = z_of(x1[U.value], x2[U.value], iw, n, m, n == 0);
+                zm[U.value] = z_of(x2[U.value], x1[U.value], iwm, m, n, false);
+            });
+            c.sstore(n, zn);
+            if (n != 0 && m != n) {
+                c.sstore(m, zm);
+            }
+        }
+    }
+}
+
 template <class Ctx, class R, int NC, int TT, int V, int S, int L, int NS, int P, int... Rest>
 __device__ __forceinline__ void ct_run(const Ctx &c, int j) {
     constexpr bool post = Ctx::kind_v == kind_r2c_half;
-    constexpr bool src_g = S == 0;
+    // c2r (even N): the pre-process fills the shared buffer, the first stage reads it
+    constexpr bool pre = S == 0 && Ctx::kind_v == kind_c2r_half;
+    constexpr bool src_g = S == 0 && !pre;
     constexpr bool dst_g = (S == L - 1) && !post;
+    if constexpr (pre) {
+        ct_c2r_pre<Ctx, R, NC, TT, V>(c, j);
+        __syncthreads();
+    }
     ct_stage<P, NS, src_g, dst_g, Ctx, R, NC, TT, V>(c, j);
     if constexpr (!dst_g) {
         __syncthreads();
