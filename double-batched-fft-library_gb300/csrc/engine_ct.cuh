@@ -578,8 +578,10 @@ __device__ __forceinline__ void ct_c2r_pre(const Ctx &c, int j) {
 template <class Ctx, class R, int NC, int TT, int V, int S, int L, int NS, int P, int... Rest>
 __device__ __forceinline__ void ct_run(const Ctx &c, int j) {
     constexpr bool post = Ctx::kind_v == kind_r2c_half;
-    // c2r (even N): the pre-process fills the shared buffer, the first stage reads it
-    constexpr bool pre = S == 0 && Ctx::kind_v == kind_c2r_half;
+    // c2r (even N): the paired pre-process fills the shared buffer and the first stage
+    // reads it, where that measured faster on GB300 (M = 8, half lengths 64, 80 and 256);
+    // elsewhere the first stage forms Z[n] in its own loads
+    constexpr bool pre = S == 0 && Ctx::kind_v == kind_c2r_half && (NC == 64 || NC == 80 || NC == 256);
     constexpr bool src_g = S == 0 && !pre;
     constexpr bool dst_g = (S == L - 1) && !post;
     if constexpr (pre) {
