@@ -128,7 +128,7 @@ def entries():
 
 # Ragged batches: float c2c N = 16..512 step 8 and r2c N = 16..512 step 8 (half length
 # 8..256 step 4), one thread per M (V = 1), as device functions of the persistent kernel.
-RAGGED_FILES = 4
+RAGGED_FILES = 6
 
 
 def ragged_entries():
@@ -176,11 +176,16 @@ def ragged_units(outdir):
                     '    __shared__ __align__(16) fft_params s_p;',
                     '    const int2 un = stage_unit_params(items, units, s_p);',
                     '    fft_tile_ct_ragged<%s>(s_p, un.y);' % targs,
+                    '}', '',
+                    '__global__ void __launch_bounds__(256, 2) plan_ct_%d(const __grid_constant__ fft_params p) {' % i,
+                    '    fft_tile_ct_ragged<%s>(p, blockIdx.x);' % targs,
                     '}', '']
-        src += ['const void *ragged_class_kernel_%d(int vid) {' % g, '    switch (vid) {']
-        for i in sorted(idx):
-            src += ['    case %d:' % i, '        return reinterpret_cast<const void *>(&ragged_class_ct_%d);' % i]
-        src += ['    default:', '        return nullptr;', '    }', '}', '', '} // namespace gbfft', '']
+        for kname in ('ragged_class_ct', 'plan_ct'):
+            src += ['const void *%s_kernel_%d(int vid) {' % (kname, g), '    switch (vid) {']
+            for i in sorted(idx):
+                src += ['    case %d:' % i, '        return reinterpret_cast<const void *>(&%s_%d);' % (kname, i)]
+            src += ['    default:', '        return nullptr;', '    }', '}', '']
+        src += ['} // namespace gbfft', '']
         fn = os.path.join(outdir, 'ragged_ct_%d.cu' % g)
         write(fn, '\n'.join(src))
         units.append(fn)
@@ -192,13 +197,16 @@ def ragged_units(outdir):
         inc += ['    case %d:' % i, '        ragged_ct_%d(p, tile);' % i, '        break;']
     inc += ['    }', '}', '']
     write(os.path.join(outdir, 'ragged_ct_dispatch.inc'), '\n'.join(inc))
-    host = ['const void *ragged_class_kernel_%d(int vid);' % g for g in range(RAGGED_FILES)]
-    host += ['', '// kernel of one class of a ragged batch (grid over the class\'s units), by table index',
-             'const void *ragged_class_kernel(int vid) {',
-             '    const void *f = nullptr;']
-    for g in range(RAGGED_FILES):
-        host += ['    if (!f) {', '        f = ragged_class_kernel_%d(vid);' % g, '    }']
-    host += ['    return f;', '}', '']
+    host = []
+    for kname, what in (('ragged_class_ct', 'one class of a ragged batch (grid over the class\'s units)'),
+                        ('plan_ct', 'a plan (grid over its tiles)')):
+        host += ['const void *%s_kernel_%d(int vid);' % (kname, g) for g in range(RAGGED_FILES)]
+        fn = 'ragged_class_kernel' if kname == 'ragged_class_ct' else 'ragged_plan_kernel'
+        host += ['', '// compile-time tile kernel of %s, by table index' % what,
+                 'const void *%s(int vid) {' % fn, '    const void *f = nullptr;']
+        for g in range(RAGGED_FILES):
+            host += ['    if (!f) {', '        f = %s_kernel_%d(vid);' % (kname, g), '    }']
+        host += ['    return f;', '}', '']
     host += ['extern const ct_entry ragged_ct_table[] = {']
     for prec, kind, nc, T, rad, V in ents:
         host.append('    {%d, %d, %d, %d, %d, %d, {%s}, nullptr, 2},' % (prec, kind, nc, T, V, len(rad), ', '.join(map(str, rad))))

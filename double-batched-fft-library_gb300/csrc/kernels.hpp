@@ -36,6 +36,8 @@ int tc_tile_transforms(int nc);
 const void *ragged_kernel_ptr(int prec, bool persistent);
 // class form of ragged batches: kernel(items, units) over the units of one class
 const void *ragged_class_kernel(int vid);
+// plan kernel (fft_params by value, one CTA per tile) of a ragged tile function
+const void *ragged_plan_kernel(int vid);
 const void *ragged_class_runtime_kernel(int prec, int kind);
 
 } // namespace gbfft

@@ -862,9 +862,9 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     if (!unrolled(rad.front())) {
         rad.insert(rad.begin(), 1);
     }
-    // ragged batches: the compile-time prime stages write shared memory only, so a prime
-    // last stage is followed by a copy stage (the same radices for the runtime engine)
-    if (q.runtime_only && !post && table_generic(rad.back())) {
+    // the compile-time prime stages write shared memory only, so a prime last stage is
+    // followed by a copy stage (the same radices for the runtime engine)
+    if (!post && table_generic(rad.back())) {
         rad.push_back(1);
     }
     // real transforms must finish all global reads of a tile before the first global write
@@ -931,12 +931,14 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
             ct = ct_lookup(q.prec, ps.kind, Nc, T, 1, rad.data(), L, minb);
         }
     }
-    // ragged batches: compile-time-size tile functions of the persistent kernel (float, V = 1)
+    // compile-time-size tile functions of the ragged set (float, V = 1): the tiles of
+    // ragged batches, and plans of lengths without a compile-time plan kernel
     int ragged_vid = -1;
-    if (!has_cb && q.runtime_only && q.prec == 4) {
+    if (!has_cb && !ct && q.prec == 4) {
         ragged_vid = ragged_ct_lookup(q.prec, ps.kind, Nc, T, 1, rad.data(), L);
         if (ragged_vid >= 0) {
             ct = &ragged_ct_table[ragged_vid];
+            V = 1;
         }
     }
     int const max_block = q.max_block > 0 ? q.max_block : (ct ? 256 : 512);
@@ -1067,7 +1069,9 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     ps.identifier = c_ident(id.str());
 
     if (!has_cb) {
-        ps.func = (ct && ct->fn) ? ct->fn : (q.prec == 4 ? kernel_f32(ps.kind) : kernel_f64(ps.kind));
+        ps.func = (ct && ct->fn) ? ct->fn
+                  : ragged_vid >= 0 ? ragged_plan_kernel(ragged_vid)
+                                    : (q.prec == 4 ? kernel_f32(ps.kind) : kernel_f64(ps.kind));
         ps.specialized = ct != nullptr;
         ps.min_blocks = ct ? ct->minb : 0;
         ps.ragged_vid = ragged_vid;

@@ -296,3 +296,25 @@ def test_full_size_round_trip(bb, po, torch_cuda, N):
     assert rel_l2(Xs.ravel(), orc) <= 2e-6
     del x, X, y
     torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize('type', [0, 1])
+def test_plans_of_the_ragged_lengths(bb, po, torch_cuda, type):
+    """Float plans of every N in {16, 24, ..., 512} (the lengths the ragged tile functions
+    cover, incl. the prime factors 17..61), forward and backward, against the oracle in FP64."""
+    torch = torch_cuda
+    rng = np.random.default_rng(7 + type)
+    for N in range(16, 513, 8):
+        M = int(rng.choice([1, 3, 8]))
+        K = int(rng.integers(1, 20))
+        for d in ([bb.FORWARD, bb.BACKWARD] if type == 0 else [bb.FORWARD]):
+            cfg = bb.configuration(1, [M, N, K], precision=bb.F32, type=type, direction=d)
+            nout = N // 2 + 1 if type == 1 else N
+            if type == 1:
+                x = rng.standard_normal(M * N * K).astype(np.float32)
+            else:
+                x = (rng.standard_normal(M * N * K) + 1j * rng.standard_normal(M * N * K)).astype(np.complex64)
+            out = run(bb, torch, cfg, x, M * nout * K, np.complex64)
+            ref = po.oracle_fft(1, [M, N, K], type, d, x.astype(np.complex128 if type == 0 else np.float64), prec=8)
+            e = rel_l2(out, ref)
+            assert e <= TOL[4], (N, M, K, d, e)
