@@ -121,9 +121,6 @@ template <class R, int Kind, int NC, int TT, int V, bool MI = false> struct ct_c
     int pshift, padd;
     bool active;
     bool live = true;
-    // coefficients (cos, -sin)(2 pi jj k / P) of a prime stage in constant memory, k-major
-    // (row k - 1, column jj - 1, H columns, rows padded with zeros to a multiple of 8)
-    const float2 *ptab = nullptr;
 
     __device__ __forceinline__ int sidx(int n) const { // LIN layout
         int i = sbase + n * p.Mb;
@@ -279,24 +276,21 @@ template <class R, int Kind, int NC, int TT, int V, bool MI = false> struct ct_c
     }
 };
 
-// Odd prime radix 17..61 (shared memory in and out, one transform per thread along M).
-// A task is one group of G output pairs (k, P-k) of one butterfly; consecutive threads
-// take consecutive butterflies of the same group, so the lanes of a warp mostly read the
-// same coefficients (one broadcast constant load per four FMAs, and one copy of the code
-// for all groups).  With s_j = x_j + x_{P-j}, d_j = x_j - x_{P-j} (the reference's pair
+// Odd prime radix 17..61 with compile-time roots of unity (shared memory in and out, one
+// transform per thread along M).  A task is one group of G output pairs (k, P-k) of one
+// butterfly; consecutive threads take consecutive butterflies of the same group, so the
+// lanes of a warp mostly run the same group and every coefficient is a literal operand
+// of its FMA.  With s_j = x_j + x_{P-j}, d_j = x_j - x_{P-j} (the reference's pair
 // optimisation, src/base/mixed_radix_fft.cpp:55-126):
 //   X_k = x_0 + sum_j cos(2 pi jk/P) s_j - i sum_j sin(2 pi jk/P) d_j,  X_{P-k} likewise.
 // The stage twiddles are applied in place first; the results stay in registers until
 // every task has read its inputs (the stage runs in place).
 __host__ __device__ constexpr bool ct_big_prime(int P) { return P > 16 && P <= 61 && P % 2 == 1; }
 
-template <int P, int G, class Ctx, class R>
-__device__ __forceinline__ void ct_prime_group(const Ctx &c, int b, int nb, int grp, cplx<R> *out) {
-    static_assert(sizeof(R) == 4, "compile-time prime stages are float");
+template <int P, int GRP, int G, class Ctx, class R>
+__device__ __forceinline__ void ct_prime_group(const Ctx &c, int b, int nb, cplx<R> *out) {
     using C = cplx<R>;
     constexpr int H = (P - 1) / 2;
-    // one row block per group: every coefficient of the group is at a literal offset
-    const float2 *w = c.ptab + grp * G * H;
     C x0[1];
     c.sload(b, x0);
     C acc[G], dd[G];
@@ -312,13 +306,19 @@ __device__ __forceinline__ void ct_prime_group(const Ctx &c, int b, int nb, int 
         c.sload(b + (P - jj) * nb, xb);
         const C sj = cadd(xa[0], xb[0]);
         const C dj = csub(xa[0], xb[0]);
-        sum = cadd(sum, sj);
+        if constexpr (GRP == 0) {
+            sum = cadd(sum, sj);
+        }
         sfor<0, G>([&](auto Q) {
-            const float2 cw = w[Q.value * H + jj - 1];
-            acc[Q.value].x += cw.x * sj.x;
-            acc[Q.value].y += cw.x * sj.y;
-            dd[Q.value].x += cw.y * dj.x;
-            dd[Q.value].y += cw.y * dj.y;
+            constexpr int k = GRP * G + decltype(Q)::value + 1;
+            if constexpr (k <= H) {
+                constexpr R cr = W<R, P, jj * k>::re; //  cos(2 pi jj k / P)
+                constexpr R ci = W<R, P, jj * k>::im; // -sin(2 pi jj k / P)
+                acc[Q.value].x += cr * sj.x;
+                acc[Q.value].y += cr * sj.y;
+                dd[Q.value].x += ci * dj.x;
+                dd[Q.value].y += ci * dj.y;
+            }
         });
     });
     out[0] = sum;
@@ -333,7 +333,7 @@ __device__ __forceinline__ void ct_stage_prime(const Ctx &c, int j) {
     using C = cplx<R>;
     constexpr int nb = NC / P;
     constexpr int H = (P - 1) / 2;
-    constexpr int G = 8; // the table's row blocks
+    constexpr int G = sizeof(R) == 4 ? 8 : 4;
     constexpr int NG = (H + G - 1) / G;
     constexpr int NT = nb * NG;
     constexpr int ITERS = (NT + TT - 1) / TT;
@@ -365,7 +365,11 @@ __device__ __forceinline__ void ct_stage_prime(const Ctx &c, int j) {
         if (live && (NT % TT == 0 || t < NT)) {
             const int grp = t / nb;
             const int b = t % nb;
-            ct_prime_group<P, G, Ctx, R>(c, b, nb, grp, out[it]);
+            sfor<0, NG>([&](auto Gi) {
+                if (grp == Gi.value) {
+                    ct_prime_group<P, Gi.value, G, Ctx, R>(c, b, nb, out[it]);
+                }
+            });
         }
     }
     __syncthreads(); // every input is read before the outputs overwrite the buffer
@@ -618,8 +622,7 @@ __device__ __forceinline__ void fft_tile_ct(const fft_params &p) {
 // The same tile for the persistent ragged kernel: tile index given, block possibly larger
 // than the tile's (Mb / V) * TT * Kb threads.
 template <class R, int Kind, int NC, int TT, int V, int... Ps>
-__device__ __forceinline__ void fft_tile_ct_ragged(const fft_params &p, long long tile,
-                                                   const float2 *ptab = nullptr) {
+__device__ __forceinline__ void fft_tile_ct_ragged(const fft_params &p, long long tile) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using Ctx = ct_ctx<R, Kind, NC, TT, V, true>;
     const int tid = threadIdx.x;
@@ -635,7 +638,7 @@ __device__ __forceinline__ void fft_tile_ct_ragged(const fft_params &p, long lon
     const long long k = kt * p.Kb + k_l;
     const int sbase = Ctx::LIN ? k_l * NC * p.Mb + m_l : k_l * NC * mvb + mv;
     Ctx c{p, reinterpret_cast<cplx<R> *>(smem_raw), m + k * p.is2, m + k * p.os2, sbase,
-          p.pad_shift, p.pad_add, live && (m < p.M) && (k < p.K), live, ptab};
+          p.pad_shift, p.pad_add, live && (m < p.M) && (k < p.K), live};
     ct_run<Ctx, R, NC, TT, V, 0, sizeof...(Ps), 1, Ps...>(c, j);
 }
 

@@ -142,45 +142,6 @@ def ragged_entries():
     return out
 
 
-def rou_float_tables():
-    """kOffset, cos and sin float literals of root_of_unity_table.cuh (exactly rounded)."""
-    import re
-    text = open(os.path.join(os.path.dirname(os.path.abspath(__file__)), 'root_of_unity_table.cuh')).read()
-    off = [int(v) for v in re.search(r'kOffset\[\d+\] = \{([^}]*)\}', text).group(1).split(',')]
-
-    def arr(name):
-        body = re.search(r'%s\[\d+\] = \{([^}]*)\}' % name, text).group(1)
-        return [v.strip() for v in body.split(',') if v.strip()]
-
-    return off, arr('kCosF'), arr('kSinF')
-
-
-def prime_tables(primes):
-    """Constant-memory coefficient tables of the compile-time prime stages (one
-    definition per prime for the whole relocatable program): for prime P, H = (P - 1) / 2
-    columns jj and rows k = 1 .. H rounded up to a multiple of 8, entry
-    (cos, -sin)(2 pi jj k / P); rows beyond H are zero."""
-    off, cs, sn = rou_float_tables()
-    neg = lambda v: v[1:] if v.startswith('-') else '-' + v
-    out = []
-    for P in sorted(primes):
-        H = (P - 1) // 2
-        rows = (H + 7) // 8 * 8
-        vals = []
-        for k in range(1, rows + 1):
-            for jj in range(1, H + 1):
-                if k <= H:
-                    q = (jj * k) % P
-                    vals.append('{%s, %s}' % (cs[off[P] + q], neg(sn[off[P] + q])))
-                else:
-                    vals.append('{0.0f, 0.0f}')
-        out.append('__constant__ float2 c_prime_%d[%d] = {' % (P, len(vals)))
-        for i in range(0, len(vals), 4):
-            out.append('    ' + ', '.join(vals[i:i + 4]) + ',')
-        out += ['};', '']
-    return out
-
-
 def write(fn, text):
     if not os.path.exists(fn) or open(fn).read() != text:
         with open(fn, 'w') as f:
@@ -204,24 +165,20 @@ def ragged_units(outdir):
     for g, idx in enumerate(groups):
         src = ['// generated by gen_specializations.py: compile-time-size tiles of the ragged kernel',
                '#include "engine_ct.cuh"', '#include "kernels.hpp"', '', 'namespace gbfft {', '']
-        src += ['extern __constant__ float2 c_prime_%d[];' % P
-                for P in sorted({r for i in idx for r in ents[i][4] if r in BIG_PRIMES})] + ['']
         for i in sorted(idx):
             prec, kind, nc, T, rad, V = ents[i]
             targs = 'float, %d, %d, %d, %d, %s' % (kind, nc, T, V, ', '.join(map(str, rad)))
-            primes = [r for r in rad if r in BIG_PRIMES]
-            tab = ', c_prime_%d' % primes[0] if primes else ''
             src += ['__device__ __noinline__ void ragged_ct_%d(const fft_params &p, long long tile) {' % i,
-                    '    fft_tile_ct_ragged<%s>(p, tile%s);' % (targs, tab),
+                    '    fft_tile_ct_ragged<%s>(p, tile);' % targs,
                     '}', '',
                     '__global__ void __launch_bounds__(256, 2) ragged_class_ct_%d(const ragged_item_dev *__restrict__ items,' % i,
                     '                                                        const int2 *__restrict__ units) {',
                     '    __shared__ __align__(16) fft_params s_p;',
                     '    const int2 un = stage_unit_params(items, units, s_p);',
-                    '    fft_tile_ct_ragged<%s>(s_p, un.y%s);' % (targs, tab),
+                    '    fft_tile_ct_ragged<%s>(s_p, un.y);' % targs,
                     '}', '',
                     '__global__ void __launch_bounds__(256, 2) plan_ct_%d(const __grid_constant__ fft_params p) {' % i,
-                    '    fft_tile_ct_ragged<%s>(p, blockIdx.x%s);' % (targs, tab),
+                    '    fft_tile_ct_ragged<%s>(p, blockIdx.x);' % targs,
                     '}', '']
         for kname in ('ragged_class_ct', 'plan_ct'):
             src += ['const void *%s_kernel_%d(int vid) {' % (kname, g), '    switch (vid) {']
@@ -232,12 +189,6 @@ def ragged_units(outdir):
         fn = os.path.join(outdir, 'ragged_ct_%d.cu' % g)
         write(fn, '\n'.join(src))
         units.append(fn)
-    tables = ['// generated by gen_specializations.py: coefficient tables of the prime stages',
-              '#include <cuda_runtime.h>', '', 'namespace gbfft {', '']
-    tables += prime_tables(BIG_PRIMES) + ['} // namespace gbfft', '']
-    fn = os.path.join(outdir, 'ragged_ct_tables.cu')
-    write(fn, '\n'.join(tables))
-    units.append(fn)
     inc = ['// generated by gen_specializations.py: compile-time-size ragged tiles', '']
     inc += ['__device__ void ragged_ct_%d(const fft_params &p, long long tile);' % i for i in range(len(ents))]
     inc += ['', '__device__ __forceinline__ void ragged_ct_call(int vid, const fft_params &p, long long tile) {',
