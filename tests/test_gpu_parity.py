@@ -318,3 +318,40 @@ def test_plans_of_the_ragged_lengths(bb, po, torch_cuda, type):
             ref = po.oracle_fft(1, [M, N, K], type, d, x.astype(np.complex128 if type == 0 else np.float64), prec=8)
             e = rel_l2(out, ref)
             assert e <= TOL[4], (N, M, K, d, e)
+
+
+@pytest.mark.parametrize('type,N,M', [(1, 160, 8), (2, 160, 8), (0, 64, 1), (2, 384, 8), (1, 96, 8)])
+def test_tuned_variants_agree(bb, po, torch_cuda, type, N, M):
+    """Every blocking the autotuner may pick (V, Mb, Kb, 2 or 3 resident CTAs) gives the
+    FP64 transform within the float tolerance."""
+    torch = torch_cuda
+    rng = np.random.default_rng(N + type)
+    K = 37
+    d = bb.BACKWARD if type == 2 else bb.FORWARD
+    cfg = bb.configuration(1, [M, N, K], precision=bb.F32, type=type, direction=d)
+    nin = N // 2 + 1 if type == 2 else N
+    nout = N // 2 + 1 if type == 1 else N
+    if type == 1:
+        x = rng.standard_normal(M * nin * K).astype(np.float32)
+    else:
+        x = (rng.standard_normal(M * nin * K) + 1j * rng.standard_normal(M * nin * K)).astype(np.complex64)
+    ref = po.oracle_fft(1, [M, N, K], type, d, x.astype(np.float64 if type == 1 else np.complex128), prec=8)
+    seen = set()
+    stream = torch.cuda.current_stream().cuda_stream
+    for V in (1, 2, 4):
+        for Mb in (1, 4, 8):
+            for Kb in (1, 4):
+                for occ in (2, 3):
+                    try:
+                        plan = bb.Plan(cfg, stream=stream, tuning=(None, 0, V, Mb, Kb, occ))
+                    except bb.BBFFTError:
+                        continue
+                    i = plan.info()
+                    key = (i.vector_width, i.mb, i.kb, i.min_blocks)
+                    if key in seen:
+                        continue
+                    seen.add(key)
+                    out = run(bb, torch, cfg, x, M * nout * K, np.float32 if type == 2 else np.complex64,
+                              plan=plan)
+                    assert rel_l2(out, ref) <= TOL[4], key
+    assert any(k[3] == 3 for k in seen) and any(k[3] == 2 for k in seen)
