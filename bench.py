@@ -627,21 +627,36 @@ def run_e2e(bb, torch, plans, prec, sptr, stream, args):
 def run_profile(args):
     """Launches for an ncu capture, no timing: `step` runs every plan of one benchmark step
     once (28 launches); `case` runs one plan once (KIND:N, KIND in r2c / c2r, float32,
-    M=8, 1 GiB real input -- or c2c:N with M=1, K=2^20)."""
+    M=8, 1 GiB real input -- or c2c:N[:FORM] with M=1, K=2^20, FORM one of native, bf16,
+    split3, split6 for the tensor-core stages); `ragged` runs the ragged batch once in
+    the class form (one kernel per tile function)."""
     import torch
 
     import bbfft_gb300 as bb
 
     stream = torch.cuda.current_stream().cuda_stream
+    if args.profile == 'ragged':
+        specs, nin, nout = ragged_specs(bb)
+        x = torch.empty(nin, dtype=torch.float32, device='cuda').uniform_(-1, 1)
+        y = torch.empty(nout, dtype=torch.float32, device='cuda')
+        r = bb.Ragged([(bb.F32, bb.FORWARD, t, N, M, K, x.data_ptr() + 4 * io, y.data_ptr() + 4 * oo)
+                       for (t, N, M, K, io, oo) in specs])
+        r.set_launch_form(r.CLASSES)
+        r.execute(stream)
+        torch.cuda.synchronize()
+        print('profiled ragged batch, units:', r.info().num_units)
+        return
+    forms = {'native': bb.COMPUTE_NATIVE, 'bf16': bb.COMPUTE_BF16,
+             'split3': bb.COMPUTE_SPLIT_BF16_3TERM, 'split6': bb.COMPUTE_SPLIT_BF16}
     if args.profile == 'step':
-        cases = [(t, N) for N in SWEEP_N for t in ('r2c', 'c2r')]
+        cases = [(t, N, 'native') for N in SWEEP_N for t in ('r2c', 'c2r')]
     else:
-        kind, n = args.profile_case.split(':')
-        cases = [(kind, int(n))]
+        f = args.profile_case.split(':')
+        cases = [(f[0], int(f[1]), f[2] if len(f) > 2 else 'native')]
     cfgs = []
-    for kind, N in cases:
+    for kind, N, form in cases:
         if kind == 'c2c':
-            cfg = bb.configuration(1, [1, N, 1 << 20], precision=bb.F32)
+            cfg = bb.configuration(1, [1, N, 1 << 20], precision=bb.F32, compute=forms[form])
             nin = nout = 2 * N * (1 << 20)
         elif kind == 'r2c':
             K = k_for(N, 4)
@@ -675,7 +690,7 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--cpu-seconds', type=float, default=15.0)
     ap.add_argument('--no-legs', action='store_true', help='headline workload only')
-    ap.add_argument('--profile', choices=['step', 'case'], help='launches for an ncu capture')
+    ap.add_argument('--profile', choices=['step', 'case', 'ragged'], help='launches for an ncu capture')
     ap.add_argument('--profile-case', default='c2r:160')
     args = ap.parse_args()
     if args.profile:
