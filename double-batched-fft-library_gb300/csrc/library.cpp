@@ -231,6 +231,12 @@ struct bbfft_cache_s {
 namespace gbfft {
 
 static std::string nvrtc_arch(int device) {
+    // device < 0: ahead-of-time compilation without a GPU, for BBFFT_GB300_AOT_ARCH
+    // (e.g. sm_103a), the counterpart of the reference tool's device option
+    if (device < 0) {
+        const char *a = std::getenv("BBFFT_GB300_AOT_ARCH");
+        return std::string("--gpu-architecture=") + (a && *a ? a : "sm_103a");
+    }
     cudaDeviceProp prop;
     GB_CUDA(cudaGetDeviceProperties(&prop, device));
     std::string arch = "sm_" + std::to_string(prop.major) + std::to_string(prop.minor);
@@ -1871,8 +1877,13 @@ int bbfft_aot_generate(const bbfft_configuration *cfgs, size_t num_cfgs, void *i
                 kernels.emplace_back(name, c.precision, kind);
             }
         }
-        int device = 0;
-        GB_CUDA(cudaGetDevice(&device));
+        // the current device's architecture, or BBFFT_GB300_AOT_ARCH when it is set (also
+        // the only way without a GPU)
+        int device = -1;
+        const char *arch = std::getenv("BBFFT_GB300_AOT_ARCH");
+        if (!(arch && *arch)) {
+            GB_CUDA(cudaGetDevice(&device));
+        }
         std::string src = gbfft::callback_program(c0.callback_source, c0.callback_length,
                                                   c0.load_function, c0.store_function, kernels);
         std::vector<char> cubin = gbfft::nvrtc_compile(src, "gbfft_aot", device);

@@ -133,10 +133,12 @@ BBFFT_GB300_API int bbfft_aot_cache_register_module(bbfft_cache_t cache, const v
                                                     size_t num_kernel_names, int device);
 /* reference: bbfft-aot-generate (tools/aot/main.cpp:22-60) over generate_fft_kernels
  * (src/base/generator.cpp:16-25).  Compiles the kernels that 1d configurations with user
- * callbacks need (all sharing one user module) into one cubin for the current device, to
- * be registered with bbfft_aot_cache_register_module; kernels of configurations without
- * callbacks are compiled into this library and need no image.  image may be NULL to query
- * *image_needed; `names` receives the kernel names, one per line. */
+ * callbacks need (all sharing one user module) into one cubin for the current device (or,
+ * when the environment variable BBFFT_GB300_AOT_ARCH names one, e.g. sm_103a, for that
+ * architecture without touching a GPU), to be registered with
+ * bbfft_aot_cache_register_module; kernels of configurations without callbacks are compiled
+ * into this library and need no image.  image may be NULL to query *image_needed; `names`
+ * receives the kernel names, one per line. */
 BBFFT_GB300_API int bbfft_aot_generate(const bbfft_configuration *cfgs, size_t num_cfgs,
                                        void *image, size_t image_len, size_t *image_needed,
                                        char *names, size_t names_len, size_t *names_needed);

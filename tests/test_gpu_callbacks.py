@@ -159,3 +159,28 @@ def test_callback_compile_error_is_reported(bb, torch_cuda):
     cfg = bb.configuration(1, [1, 16, 1], precision=4, callbacks=('this is not C++', 'load', None))
     with pytest.raises(bb.CompileError, match='NVRTC'):
         bb.make_plan(cfg)
+
+
+def test_aot_tool_image_serves_plans(bb, torch_cuda, tmp_path):
+    """An image written by the bbfft_gb300.aot tool (offline, --arch of this GPU) and loaded
+    with aot.load() serves plan creation without NVRTC; results equal the JIT plan's."""
+    torch = torch_cuda
+    from bbfft_gb300 import aot
+
+    major, minor = torch.cuda.get_device_capability()
+    src = tmp_path / 'user.cu'
+    src.write_text(LOAD_SRC.format(T2='float2', M=4, NEXT=64 // 2 + 1, NCUT=20))
+    out = tmp_path / 'k.cubin'
+    aot.main(['-o', str(out), '--callbacks', str(src), '--load', 'load_id',
+              '--arch', 'sm_%d%da' % (major, minor), 'srbo4.64*8'])
+    cache = aot.load(str(out), device=torch.cuda.current_device())
+    cfg = bb.configuration(1, [4, 64, 8], precision=4, type=bb.C2R, direction=bb.BACKWARD,
+                           callbacks=(src.read_text(), 'load_id', None))
+    stream = torch.cuda.current_stream().cuda_stream
+    p_aot = bb.Plan(cfg, stream=stream, cache=cache)
+    assert cache.stats() == (1, 0)
+    rng = np.random.default_rng(8)
+    X = (rng.standard_normal(4 * 33 * 8) + 1j * rng.standard_normal(4 * 33 * 8)).astype(np.complex64)
+    y_aot = run(bb, torch, cfg, X, 4 * 64 * 8, np.float32, plan=p_aot)
+    y_jit = run(bb, torch, cfg, X, 4 * 64 * 8, np.float32)
+    assert np.array_equal(y_aot, y_jit)
