@@ -41,16 +41,25 @@ def tune_config(torch, prec, type, N, M, K, reps=4, verbose=False):
     results = {}
     mbs = sorted({m for m in (M, 64, 32, 16, 8, 4, 2, 1) if m <= M and m <= 64}, reverse=True)
     occs = (2, 3) if prec == 4 else (2,)
-    for V in (0, 1, 2, 4):
+    stages = [(None, 0)]
+    if prec == 4 and type != bb.C2C and N % 2 == 0:
+        stages += [(tuple(r), t) for r, t in alt_stages().get(N // 2, [])]
+    for rad, T in stages:
+     for V in (0, 1, 2, 4):
         for Mb in mbs:
             for Kb in (0, 1, 2, 4, 8, 16, 32, 64, 128, 256):
               for occ in occs:
                 try:
-                    plan = bb.Plan(cfg, stream=stream.cuda_stream, tuning=(None, 0, V, Mb, Kb, occ))
+                    plan = bb.Plan(cfg, stream=stream.cuda_stream,
+                                   tuning=(list(rad) if rad else None, T, V, Mb, Kb, occ))
                 except bb.BBFFTError:
                     continue
                 info = plan.info()
-                key = (info.vector_width, info.mb, info.kb, info.min_blocks or 2)
+                if rad and not info.specialized:
+                    plan.destroy()
+                    continue  # only the compile-time kernels of the alternatives are worth timing
+                key = (info.vector_width, info.mb, info.kb, info.min_blocks or 2,
+                       tuple(info.radix[:info.num_stages]) if rad else (), info.threads_per_transform if rad else 0)
                 if key in results:
                     continue
                 for _ in range(2):
@@ -70,12 +79,13 @@ def tune_config(torch, prec, type, N, M, K, reps=4, verbose=False):
     kind = re.match(r'gbfft_f\d+_([a-z0-9]+)_', ident).group(1)
     nbytes = (n_in * (prec if type == bb.R2C else 2 * prec) + n_out * (prec if type == bb.C2R else 2 * prec)) * M * K
     gbs = nbytes / (results[best_key][0] * 1e-3) / 1e9
-    entry = (prec, kind, N, M) + best_key
+    entry = (prec, kind, N, M) + best_key[:4] + (best_key[5], 'x'.join(map(str, best_key[4])))
     if verbose:
         worst = max(r[0] for r in results.values())
-        print('prec %d type %d N %4d M %4d: best V=%d Mb=%d Kb=%d occ=%d %.1f GB/s (%d candidates, '
-              'worst %.2fx)' % (prec, type, N, M, best_key[0], best_key[1], best_key[2], best_key[3],
-                                gbs, len(results), worst / results[best_key][0]), flush=True)
+        print('prec %d type %d N %4d M %4d: best V=%d Mb=%d Kb=%d occ=%d T=%d rad=%s %.1f GB/s (%d '
+              'candidates, worst %.2fx)' % (prec, type, N, M, best_key[0], best_key[1], best_key[2],
+                                            best_key[3], best_key[5], best_key[4] or 'auto', gbs,
+                                            len(results), worst / results[best_key][0]), flush=True)
     return entry, gbs
 
 
@@ -102,6 +112,17 @@ def default_configs(quick=False):
     return cfgs
 
 
+def alt_stages():
+    """Alternative (radices, threads per transform) with compile-time kernels, by half length
+    (csrc/gen_specializations.py ALT_STAGES)."""
+    csrc = os.path.join(os.path.dirname(HERE), 'csrc')
+    if csrc not in sys.path:
+        sys.path.insert(0, csrc)
+    import gen_specializations
+
+    return gen_specializations.ALT_STAGES
+
+
 def read_table(path):
     """Entries of an existing table as (prec, kind, N, M, V, Mb, Kb, occ), GB/s."""
     out = []
@@ -113,7 +134,9 @@ def read_table(path):
         if len(f) < 7:
             continue
         occ = int(f[7]) if len(f) > 7 else 2
-        e = (int(f[0]), f[1], int(f[2]), int(f[3]), int(f[4]), int(f[5]), int(f[6]), occ)
+        T = int(f[8]) if len(f) > 9 else 0
+        rad = f[9] if len(f) > 9 else ''
+        e = (int(f[0]), f[1], int(f[2]), int(f[3]), int(f[4]), int(f[5]), int(f[6]), occ, T, rad)
         try:
             gbs = float(note.strip())
         except ValueError:
@@ -124,10 +147,14 @@ def read_table(path):
 
 def write_table(path, entries):
     os.makedirs(os.path.dirname(path), exist_ok=True)
-    lines = ['# bbfft GB300 tuning table: <prec bytes> <kind> <N> <M> <V> <Mb> <Kb> <CTAs per SM>  # GB/s',
+    lines = ['# bbfft GB300 tuning table: <prec bytes> <kind> <N> <M> <V> <Mb> <Kb> <CTAs per SM> '
+             '[<threads per transform> <radices AxB>]  # GB/s',
              '# written by bbfft_gb300/autotune.py from CUDA-event timings on a GB300']
     for e, gbs in entries:
-        lines.append('%d %s %d %d %d %d %d %d  # %.1f' % (e + (gbs,)))
+        head = '%d %s %d %d %d %d %d %d' % e[:8]
+        if len(e) > 9 and e[9]:
+            head += ' %d %s' % (e[8], e[9])
+        lines.append('%s  # %.1f' % (head, gbs))
     with open(path, 'w') as f:
         f.write('\n'.join(lines) + '\n')
 

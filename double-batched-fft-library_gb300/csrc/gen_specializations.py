@@ -109,6 +109,16 @@ def vector_width(prec, rad):
     return v
 
 
+# Alternative radices / threads per transform for the float real half lengths whose default
+# stages leave threads idle (the autotuner picks among them): a stage with nb butterflies
+# over T threads runs ceil(nb / T) rounds.
+ALT_STAGES = {
+    80: [([10, 8], 10), ([8, 10], 8), ([8, 10], 10), ([16, 5], 5), ([5, 16], 5)],
+    112: [([16, 7], 16), ([7, 16], 7), ([7, 16], 16), ([4, 4, 7], 28)],
+    192: [([8, 6, 4], 32), ([16, 12], 12), ([12, 16], 12), ([16, 12], 16), ([4, 6, 8], 48)],
+}
+
+
 def entries():
     out = []
     for prec in (4, 8):
@@ -118,11 +128,15 @@ def entries():
                 rad, T = stage_list(nc, kind)
                 if any(r not in UNROLLED for r in rad):
                     continue
-                for V in sorted({1, vector_width(prec, rad)}):
-                    # resident CTAs the register allocation is sized for: 2 (up to 128
-                    # registers), and for float also 3 (up to 80), chosen by the autotuner
-                    for minb in ((2, 3) if prec == 4 else (2,)):
-                        out.append((prec, kind, nc, T, rad, V, minb))
+                variants = [(rad, T)]
+                if prec == 4 and kind in (1, 3):
+                    variants += ALT_STAGES.get(nc, [])
+                for rad, T in variants:
+                    for V in sorted({1, vector_width(prec, rad)}):
+                        # resident CTAs the register allocation is sized for: 2 (up to 128
+                        # registers), and for float also 3 (up to 80), chosen by the autotuner
+                        for minb in ((2, 3) if prec == 4 else (2,)):
+                            out.append((prec, kind, nc, T, rad, V, minb))
     return out
 
 

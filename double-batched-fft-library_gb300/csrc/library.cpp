@@ -429,7 +429,9 @@ struct pass_request {
 
 struct tune_entry {
     int V, Mb, Kb;
-    int occ; // resident CTAs the kernel's registers are sized for (2 or 3)
+    int occ;              // resident CTAs the kernel's registers are sized for (2 or 3)
+    int T;                // threads per transform (0: the heuristic's)
+    std::vector<int> rad; // radices (empty: the heuristic's)
 };
 
 static std::string library_dir() {
@@ -459,14 +461,25 @@ static std::map<std::tuple<int, std::string, int, long long>, tune_entry> const 
                 line = line.substr(0, hash);
             }
             std::istringstream ls(line);
-            int prec, N, V, Mb, Kb, occ = 2;
+            int prec, N, V, Mb, Kb, occ = 2, T = 0;
             long long M;
-            std::string kind;
+            std::string kind, rads;
             if (ls >> prec >> kind >> N >> M >> V >> Mb >> Kb) {
+                // optional columns: CTAs per SM, threads per transform, radices (AxBxC)
                 if (!(ls >> occ) || (occ != 2 && occ != 3)) {
-                    occ = 2; // optional eighth column
+                    occ = 2;
                 }
-                table[std::make_tuple(prec, kind, N, M)] = tune_entry{V, Mb, Kb, occ};
+                std::vector<int> rad;
+                if (ls >> T >> rads) {
+                    std::istringstream rs(rads);
+                    std::string tok;
+                    while (std::getline(rs, tok, 'x')) {
+                        rad.push_back(std::atoi(tok.c_str()));
+                    }
+                } else {
+                    T = 0;
+                }
+                table[std::make_tuple(prec, kind, N, M)] = tune_entry{V, Mb, Kb, occ, T, rad};
             }
         }
     });
@@ -816,7 +829,21 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     int Nc = (is_real && even) ? N / 2 : N;
     int Nt = (is_real && even) ? N : Nc;
 
-    std::vector<int> rad = q.radices.empty() ? choose_radices(Nc) : q.radices;
+    // autotuned blocking (radices, threads per transform, V, Mb, Kb, register budget)
+    tune_entry const *te = nullptr;
+    if (q.radices.empty() && q.T == 0 && q.V == 0 && q.Mb == 0 && q.Kb == 0 && q.occ == 0 &&
+        !q.force_v1 && !q.runtime_only && q.compute == BBFFT_COMPUTE_NATIVE) {
+        te = find_tuning(q.prec, ps.kind, N, q.M);
+    }
+    bool te_rad = false;
+    if (te && !te->rad.empty()) {
+        long long prod = 1;
+        for (int r : te->rad) {
+            prod *= r > 0 ? r : 0;
+        }
+        te_rad = prod == Nc; // a table line for another length is ignored
+    }
+    std::vector<int> rad = !q.radices.empty() ? q.radices : te_rad ? te->rad : choose_radices(Nc);
     {
         long long prod = 1;
         for (int r : rad) {
@@ -888,7 +915,8 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
             pu = std::max(pu, r);
         }
     }
-    int T = q.T > 0 ? q.T : std::max(1, Nc / pu);
+    int const reqT = q.T > 0 ? q.T : (te && (te_rad || te->rad.empty()) ? te->T : 0);
+    int T = reqT > 0 ? reqT : std::max(1, Nc / pu);
     if (pu == 1) {
         T = std::min(Nc, 64);
     }
@@ -900,7 +928,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
             ptg = std::max(ptg, r);
         }
     }
-    if (ptg > 0 && q.T <= 0) {
+    if (ptg > 0 && reqT <= 0) {
         int H = (ptg - 1) / 2;
         T = Nc / ptg * ((H + gen_group - 1) / gen_group);
     }
@@ -909,14 +937,11 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     long long M = q.M, K = q.K;
     bool has_cb = (q.load_fn && *q.load_fn) || (q.store_fn && *q.store_fn);
     int reqV = q.V, reqMb = q.Mb, reqKb = q.Kb, reqOcc = q.occ;
-    if (q.radices.empty() && q.T == 0 && q.V == 0 && q.Mb == 0 && q.Kb == 0 && q.occ == 0 &&
-        !q.force_v1 && !q.runtime_only) {
-        if (auto te = find_tuning(q.prec, ps.kind, N, M)) {
-            reqV = te->V;
-            reqMb = te->Mb;
-            reqKb = te->Kb;
-            reqOcc = te->occ;
-        }
+    if (te) {
+        reqV = te->V;
+        reqMb = te->Mb;
+        reqKb = te->Kb;
+        reqOcc = te->occ;
     }
     int const minb = reqOcc == 3 ? 3 : 2;
     // compile-time-size kernel, vectorised over M when the layout allows it
