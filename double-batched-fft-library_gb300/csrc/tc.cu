@@ -25,11 +25,32 @@ namespace tc {
 constexpr int kThreads = 256;
 constexpr int kElems = 2048; // complex elements per CTA tile
 
-__device__ __forceinline__ int pad(int i) { return i + (i >> 4); }
+// padded shared index: three spare elements per 16 (per 8 for length 256), which keeps a
+// warp's 8-byte accesses of every stage at about 2.5 wavefronts (2 is the minimum)
+template <int NC> __host__ __device__ constexpr int pad(int i) {
+    return NC == 256 ? i + (i >> 3) * 3 : i + (i >> 4) * 3;
+}
+constexpr int kBufElems = kElems + (kElems >> 3) * 3 + 8; // covers every length's padding
 
 __device__ __forceinline__ unsigned pack(__nv_bfloat16 lo, __nv_bfloat16 hi) {
     return static_cast<unsigned>(__bfloat16_as_ushort(lo)) |
            (static_cast<unsigned>(__bfloat16_as_ushort(hi)) << 16);
+}
+
+// splits (x0, x1) into PIECES packed bfloat16 pairs whose sums approximate x0 and x1 (one
+// paired conversion per piece; the low half holds x0)
+template <int PIECES> __device__ __forceinline__ void split2(float x0, float x1, unsigned *out) {
+    float r0 = x0, r1 = x1;
+#pragma unroll
+    for (int i = 0; i < PIECES; ++i) {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(r0, r1);
+        const unsigned u = *reinterpret_cast<const unsigned *>(&h);
+        out[i] = u;
+        if (i + 1 < PIECES) {
+            r0 -= __uint_as_float(u << 16);
+            r1 -= __uint_as_float(u & 0xffff0000u);
+        }
+    }
 }
 
 // splits x into PIECES bfloat16 numbers whose sum approximates x
@@ -116,7 +137,7 @@ __device__ __forceinline__ void stage16(const float2 *src, float2 *dst, int Ns, 
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const int r = 2 * q + (u & 1) + 8 * (u >> 1); // 2q, 2q+1, 2q+8, 2q+9
-                float2 v = src[pad(tt[h] * NC + bb[h] + r * nb)];
+                float2 v = src[pad<NC>(tt[h] * NC + bb[h] + r * nb)];
                 if (Ns > 1 && r > 0) {
                     v = cmul(v, __ldg(tw + r * kk * twstride));
                 }
@@ -128,20 +149,18 @@ __device__ __forceinline__ void stage16(const float2 *src, float2 *dst, int Ns, 
         unsigned a[PIECES][2][4];
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
-            __nv_bfloat16 p[2][4][PIECES];
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    split<PIECES>(s == 0 ? xr[h][u] : xi[h][u], p[h][u]);
-                }
-            }
+            const float(*x)[4] = s == 0 ? xr : xi;
+            unsigned t[4][PIECES];
+            split2<PIECES>(x[0][0], x[0][1], t[0]); // row g, cols 2q, 2q+1
+            split2<PIECES>(x[1][0], x[1][1], t[1]); // row g+8
+            split2<PIECES>(x[0][2], x[0][3], t[2]); // row g, cols 2q+8, 2q+9
+            split2<PIECES>(x[1][2], x[1][3], t[3]); // row g+8
 #pragma unroll
             for (int pc = 0; pc < PIECES; ++pc) {
-                a[pc][s][0] = pack(p[0][0][pc], p[0][1][pc]); // row g, cols 2q, 2q+1
-                a[pc][s][1] = pack(p[1][0][pc], p[1][1][pc]); // row g+8
-                a[pc][s][2] = pack(p[0][2][pc], p[0][3][pc]); // row g, cols 2q+8, 2q+9
-                a[pc][s][3] = pack(p[1][2][pc], p[1][3][pc]); // row g+8
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    a[pc][s][r] = t[r][pc];
+                }
             }
         }
         float d[4][4];
@@ -172,7 +191,7 @@ __device__ __forceinline__ void stage16(const float2 *src, float2 *dst, int Ns, 
                 const int jr = (u >> 1);    // n-tile of the real part
                 const int ji = 2 + (u >> 1); // n-tile of the imaginary part
                 const int e = (u & 1) + 2 * h;
-                dst[pad(tt[h] * NC + o + k * Ns)] = mk<float>(d[jr][e], d[ji][e]);
+                dst[pad<NC>(tt[h] * NC + o + k * Ns)] = mk<float>(d[jr][e], d[ji][e]);
             }
         }
     }
@@ -190,7 +209,7 @@ __device__ __forceinline__ void stage_last(const float2 *src, float2 *out, int N
         float2 v[P];
         const int kk = b % Ns;
         sfor<0, P>([&](auto I) {
-            v[I.value] = src[pad(t * NC + b + I.value * nb)];
+            v[I.value] = src[pad<NC>(t * NC + b + I.value * nb)];
             if (I.value > 0) {
                 v[I.value] = cmul(v[I.value], __ldg(tw + I.value * kk * twstride));
             }
@@ -210,11 +229,11 @@ __device__ __forceinline__ void stage_last(const float2 *src, float2 *out, int N
 }
 
 // c2c float, M = 1, packed: tiles of kElems / NC transforms per CTA.
-template <int PIECES, int NC> __global__ void __launch_bounds__(kThreads) fft_tc_kernel(const __grid_constant__ fft_params p) {
+template <int PIECES, int NC> __global__ void __launch_bounds__(kThreads, 3) fft_tc_kernel(const __grid_constant__ fft_params p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int tiles = kElems / NC;
     float2 *buf0 = reinterpret_cast<float2 *>(smem_raw);
-    float2 *buf1 = buf0 + pad(kElems) + 8;
+    float2 *buf1 = buf0 + kBufElems;
     const float2 *tw = static_cast<const float2 *>(p.tw);
     const bool conj_in = p.flags & flag_conj_in, conj_out = p.flags & flag_conj_out;
     const long long t0 = static_cast<long long>(blockIdx.x) * tiles;
@@ -233,8 +252,8 @@ template <int PIECES, int NC> __global__ void __launch_bounds__(kThreads) fft_tc
             v.y = -v.y;
             v.w = -v.w;
         }
-        buf0[pad(2 * i)] = mk<float>(v.x, v.y);
-        buf0[pad(2 * i + 1)] = mk<float>(v.z, v.w);
+        buf0[pad<NC>(2 * i)] = mk<float>(v.x, v.y);
+        buf0[pad<NC>(2 * i + 1)] = mk<float>(v.z, v.w);
     }
     __syncthreads();
     stage16<PIECES, NC>(buf0, buf1, 1, tw, B, tiles);
@@ -250,7 +269,7 @@ template <int PIECES, int NC> __global__ void __launch_bounds__(kThreads) fft_tc
             float2 *yt = y + t0 * NC;
             for (int i = threadIdx.x; i < kElems / 2; i += kThreads) {
                 if (2 * i < nt * NC) {
-                    float2 a = buf0[pad(2 * i)], b = buf0[pad(2 * i + 1)];
+                    float2 a = buf0[pad<NC>(2 * i)], b = buf0[pad<NC>(2 * i + 1)];
                     if (conj_out) {
                         a.y = -a.y;
                         b.y = -b.y;
@@ -264,7 +283,7 @@ template <int PIECES, int NC> __global__ void __launch_bounds__(kThreads) fft_tc
 
 } // namespace tc
 
-std::size_t tc_shared_bytes() { return (2 * (static_cast<std::size_t>(tc::kElems) + tc::kElems / 16) + 16) * 8; }
+std::size_t tc_shared_bytes() { return 2 * static_cast<std::size_t>(tc::kBufElems) * 8; }
 int tc_tile_transforms(int nc) { return tc::kElems / nc; }
 
 const void *tc_kernel(int pieces, int nc) {
