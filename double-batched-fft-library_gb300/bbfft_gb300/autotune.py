@@ -41,6 +41,8 @@ def tune_config(torch, prec, type, N, M, K, reps=4, verbose=False):
     results = {}
     mbs = sorted({m for m in (M, 64, 32, 16, 8, 4, 2, 1) if m <= M and m <= 64}, reverse=True)
     occs = (2, 3) if prec == 4 else (2,)
+    if prec == 4 and type == bb.C2R and N % 2 == 0:
+        occs += (12, 13)  # paired c2r pre-process variants
     stages = [(None, 0)]
     if prec == 4 and type != bb.C2C and N % 2 == 0:
         stages += [(tuple(r), t) for r, t in alt_stages().get(N // 2, [])]

@@ -101,12 +101,14 @@ template <int V> __device__ __forceinline__ void stv(double *p, const double *o)
     }
 }
 
-template <class R, int Kind, int NC, int TT, int V, bool MI = false> struct ct_ctx {
+template <class R, int Kind, int NC, int TT, int V, bool MI = false, bool PAIR = false> struct ct_ctx {
     using C = cplx<R>;
     static constexpr int kind_v = Kind;
     // may_idle: the block has more threads than the tile (persistent ragged kernel); the
     // threads beyond the tile (live == false) only take part in the barriers
     static constexpr bool may_idle = MI;
+    // c2r (even N): form Z[n] and Z[NC-n] together in a pre-pass into shared memory
+    static constexpr bool paired_c2r = PAIR;
     static constexpr bool half = Kind == kind_r2c_half || Kind == kind_c2r_half;
     static constexpr int NN = half ? 2 * NC : NC; // logical length (odd kinds: N = NC)
     // lane vectors of 16 bytes or more are stored as 16-byte chunks in NQ planes with an
@@ -578,10 +580,9 @@ __device__ __forceinline__ void ct_c2r_pre(const Ctx &c, int j) {
 template <class Ctx, class R, int NC, int TT, int V, int S, int L, int NS, int P, int... Rest>
 __device__ __forceinline__ void ct_run(const Ctx &c, int j) {
     constexpr bool post = Ctx::kind_v == kind_r2c_half;
-    // c2r (even N): the paired pre-process fills the shared buffer and the first stage
-    // reads it, where that measured faster on GB300 (M = 8, half lengths 64, 80 and 256);
-    // elsewhere the first stage forms Z[n] in its own loads
-    constexpr bool pre = S == 0 && Ctx::kind_v == kind_c2r_half && (NC == 64 || NC == 80 || NC == 256);
+    // c2r (even N), paired variant: the pre-process fills the shared buffer and the first
+    // stage reads it; otherwise the first stage forms Z[n] in its own loads
+    constexpr bool pre = S == 0 && Ctx::kind_v == kind_c2r_half && Ctx::paired_c2r;
     constexpr bool src_g = S == 0 && !pre;
     constexpr bool dst_g = (S == L - 1) && !post;
     if constexpr (pre) {
@@ -599,10 +600,10 @@ __device__ __forceinline__ void ct_run(const Ctx &c, int j) {
     }
 }
 
-template <class R, int Kind, int NC, int TT, int V, int... Ps>
+template <class R, int Kind, int NC, int TT, int V, bool PAIR, int... Ps>
 __device__ __forceinline__ void fft_tile_ct(const fft_params &p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    using Ctx = ct_ctx<R, Kind, NC, TT, V>;
+    using Ctx = ct_ctx<R, Kind, NC, TT, V, false, PAIR>;
     const int tid = threadIdx.x;
     const int mvb = p.Mb / V;
     const int mv = tid % mvb;

@@ -17,6 +17,7 @@ EVEN_NC = [2, 4, 8, 16, 32, 64, 128, 256, 512, 24, 48, 80, 96, 112, 160, 192, 22
 ODD_NC = [3, 5, 7, 9, 11, 13, 15, 25, 27]
 KINDS = {0: 'c2c', 1: 'r2ch', 2: 'r2cf', 3: 'c2rh', 4: 'c2rf'}
 UNROLLED = set(range(1, 14)) | {16}
+UNIT_KERNELS = 48
 
 
 def prime_factors(n):
@@ -133,9 +134,13 @@ def entries():
                     variants += ALT_STAGES.get(nc, [])
                 for rad, T in variants:
                     for V in sorted({1, vector_width(prec, rad)}):
-                        # resident CTAs the register allocation is sized for: 2 (up to 128
-                        # registers), and for float also 3 (up to 80), chosen by the autotuner
-                        for minb in ((2, 3) if prec == 4 else (2,)):
+                        # kernel variant: resident CTAs the register allocation is sized for,
+                        # 2 (up to 128 registers) and for float also 3 (up to 80); plus 10 for
+                        # the paired c2r pre-process (float c2r, even N).  The autotuner picks.
+                        minbs = (2, 3) if prec == 4 else (2,)
+                        if prec == 4 and kind == 3:
+                            minbs += (12, 13)
+                        for minb in minbs:
                             out.append((prec, kind, nc, T, rad, V, minb))
     return out
 
@@ -250,24 +255,31 @@ def main(outdir):
     files = {}
     for prec, kind, nc, T, rad, V, minb in ents:
         files.setdefault((prec, kind), []).append((nc, T, rad, V, minb))
+    # units of at most UNIT_KERNELS kernels, compiled in parallel
+    split = {}
+    for (prec, kind), lst in files.items():
+        n = (len(lst) + UNIT_KERNELS - 1) // UNIT_KERNELS
+        for part in range(n):
+            split[(prec, kind, part)] = lst[part::n]
+    files = split
     index = ['// generated by gen_specializations.py', '#include "kernels.hpp"', '',
              'namespace gbfft {']
     tables = []
-    for (prec, kind), lst in sorted(files.items()):
+    for (prec, kind, part), lst in sorted(files.items()):
         R = 'float' if prec == 4 else 'double'
-        name = 'ct_table_f%d_%s' % (prec * 8, KINDS[kind])
+        name = 'ct_table_f%d_%s_%d' % (prec * 8, KINDS[kind], part)
         src = ['// generated by gen_specializations.py: compile-time-size FFT kernels',
                '#include "engine_ct.cuh"', '#include "kernels.hpp"', '', 'namespace gbfft {', '',
                'template <class R, int Kind, int NC, int TT, int V, int MINB, int... Ps>',
-               '__global__ void __launch_bounds__(256, MINB) fft_kernel_ct(const __grid_constant__ fft_params p) {',
-               '    fft_tile_ct<R, Kind, NC, TT, V, Ps...>(p);', '}', '',
+               '__global__ void __launch_bounds__(256, MINB % 10) fft_kernel_ct(const __grid_constant__ fft_params p) {',
+               '    fft_tile_ct<R, Kind, NC, TT, V, (MINB >= 10), Ps...>(p);', '}', '',
                'extern const ct_entry %s[] = {' % name]
         for nc, T, rad, V, minb in lst:
             rs = ', '.join(map(str, rad))
             src.append('    {%d, %d, %d, %d, %d, %d, {%s}, reinterpret_cast<const void *>(&fft_kernel_ct<%s, %d, %d, %d, %d, %d, %s>), %d},'
                        % (prec, kind, nc, T, V, len(rad), rs, R, kind, nc, T, V, minb, rs, minb))
         src += ['};', 'extern const int %s_size = %d;' % (name, len(lst)), '', '} // namespace gbfft', '']
-        fn = os.path.join(outdir, 'kernels_ct_f%d_%s.cu' % (prec * 8, KINDS[kind]))
+        fn = os.path.join(outdir, 'kernels_ct_f%d_%s_%d.cu' % (prec * 8, KINDS[kind], part))
         text = '\n'.join(src)
         if not os.path.exists(fn) or open(fn).read() != text:
             with open(fn, 'w') as f:
@@ -305,7 +317,7 @@ def main(outdir):
     if not os.path.exists(fn) or open(fn).read() != text:
         with open(fn, 'w') as f:
             f.write(text)
-    return (sorted(os.path.join(outdir, 'kernels_ct_f%d_%s.cu' % (p * 8, KINDS[k])) for p, k in files),
+    return (sorted(os.path.join(outdir, 'kernels_ct_f%d_%s_%d.cu' % (p * 8, KINDS[k], n)) for p, k, n in files),
             rag_units)
 
 

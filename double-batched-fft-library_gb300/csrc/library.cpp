@@ -466,7 +466,7 @@ static std::map<std::tuple<int, std::string, int, long long>, tune_entry> const 
             std::string kind, rads;
             if (ls >> prec >> kind >> N >> M >> V >> Mb >> Kb) {
                 // optional columns: CTAs per SM, threads per transform, radices (AxBxC)
-                if (!(ls >> occ) || (occ != 2 && occ != 3)) {
+                if (!(ls >> occ) || (occ != 2 && occ != 3 && occ != 12 && occ != 13)) {
                     occ = 2;
                 }
                 std::vector<int> rad;
@@ -943,7 +943,11 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         reqKb = te->Kb;
         reqOcc = te->occ;
     }
-    int const minb = reqOcc == 3 ? 3 : 2;
+    // kernel variant: 2 / 3 resident CTAs, + 10 for the paired c2r pre-process
+    int minb = (reqOcc == 3 || reqOcc == 13) ? 3 : 2;
+    if ((reqOcc == 12 || reqOcc == 13) && ps.kind == kind_c2r_half && q.prec == 4) {
+        minb += 10;
+    }
     // compile-time-size kernel, vectorised over M when the layout allows it
     const ct_entry *ct = nullptr;
     int V = 1;
@@ -1104,7 +1108,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
                   : ragged_vid >= 0 ? ragged_plan_kernel(ragged_vid)
                                     : (q.prec == 4 ? kernel_f32(ps.kind) : kernel_f64(ps.kind));
         ps.specialized = ct != nullptr;
-        ps.min_blocks = ct ? ct->minb : 0;
+        ps.min_blocks = ct ? ct->minb : 0; // (+ 10: paired c2r variant)
         ps.ragged_vid = ragged_vid;
         if (V > 1) {
             pass_request q1 = q;
