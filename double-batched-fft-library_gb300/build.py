@@ -22,7 +22,7 @@ LIB = os.path.join(OUTDIR, 'libbbfft_gb300.so')
 
 ARCH = '-gencode=arch=compute_103a,code=sm_103a'
 ENGINE_HEADERS = ['params.h', 'root_of_unity_table.cuh', 'radix.cuh', 'engine.cuh']
-KERNEL_UNITS = ['kernels_f32.cu', 'kernels_f64.cu', 'noalloc.cu', 'tc.cu']
+KERNEL_UNITS = ['kernels_f32.cu', 'kernels_f64.cu', 'noalloc.cu', 'tc.cu', 'strided_copy.cu']
 # relocatable device code, linked with nvcc -dlink: the persistent ragged kernel calls the
 # compile-time-size tile functions of the generated ragged_ct_<i>.cu units
 RDC_UNITS = ['ragged.cu']

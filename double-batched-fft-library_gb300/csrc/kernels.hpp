@@ -34,6 +34,19 @@ int tc_tile_transforms(int nc);
 
 // persistent kernel of ragged batches (ragged.cu)
 const void *ragged_kernel_ptr(int prec, bool persistent);
+
+// strided gather / scatter of nd plans with non-default layouts (strided_copy.cu)
+constexpr int copy_max_rank = 5;
+struct copy_params {
+    const void *src;
+    void *dst;
+    long long total;                  // elements
+    long long shape[copy_max_rank];   // packed side, mode 0 fastest
+    long long stride[copy_max_rank];  // strided side (elements)
+    int rank;
+    int gather;                       // 1: strided src -> packed dst; 0: packed src -> strided dst
+};
+const void *strided_copy_kernel_ptr(int elem_bytes);
 // class form of ragged batches: kernel(items, units) over the units of one class
 const void *ragged_class_kernel(int vid);
 // plan kernel (fft_params by value, one CTA per tile) of a ragged tile function

@@ -397,8 +397,10 @@ struct pass {
     int ragged_vid = -1;              // compile-time-size tile of the ragged kernel, or -1
     int min_blocks = 0;               // register budget of the compile-time kernel (0: none)
     std::string identifier;
-    int in_sel = 0;  // 0: user input, 2: temporary
-    int out_sel = 1; // 1: user output, 2: temporary
+    int in_sel = 0;  // 0: user input, 2: temporary, 3: packed input, 4: packed output
+    int out_sel = 1; // 1: user output, 2: temporary, 3: packed input, 4: packed output
+    bool copy = false; // strided gather / scatter of an nd plan with a non-default layout
+    copy_params cp = {};
 };
 
 struct pass_request {
@@ -1296,6 +1298,8 @@ struct bbfft_plan_s {
     cudaStream_t stream = nullptr;
     std::vector<gbfft::pass> passes;
     std::shared_ptr<gbfft::device_buffer> tmp;
+    // nd plans with non-default layouts run on packed copies of the input and output
+    std::shared_ptr<gbfft::device_buffer> packed_in, packed_out;
     bool inplace_ok = true;
     bool jit = false;
 };
@@ -1360,12 +1364,19 @@ static void make_plan_impl(bbfft_configuration const &cfg, cudaStream_t stream,
         }
         return true;
     };
+    // nd with a layout other than the two defaults: gather the input into the packed
+    // out-of-place layout, run the chain there and scatter the result (the reference rejects
+    // such layouts, src/common/algorithm/nd_fft.hpp:47-49)
+    bool strided_nd = false;
     if (cfg.dim > 1) {
         if (has_cb) {
             bad_config("User modules are unsuported for FFT dimension > 1.");
         }
         if (!is_default(false) && !is_default(true)) {
-            bad_config("Only default tensor layouts are supported for the nd_fft.");
+            if (adjoint) {
+                bad_config("adjoint plans of nd transforms need a default tensor layout");
+            }
+            strided_nd = true;
         }
     }
     if (adjoint && has_cb) {
@@ -1404,7 +1415,7 @@ static void make_plan_impl(bbfft_configuration const &cfg, cudaStream_t stream,
         return;
     }
     // ---- nd: chain of 1d passes (reference src/common/algorithm/nd_fft.hpp:27-130) ----
-    bool inplace_layout = is_default(true);
+    bool inplace_layout = !strided_nd && is_default(true);
     bool is_real = cfg.type != BBFFT_C2C;
     unsigned dim = cfg.dim;
     auto nd_complex = [&](unsigned d) -> long long {
@@ -1468,8 +1479,10 @@ static void make_plan_impl(bbfft_configuration const &cfg, cudaStream_t stream,
     std::size_t real_b = cfg.precision, cplx_b = 2 * real_b;
     bool in_real = adjoint ? cfg.type == BBFFT_C2R : cfg.type == BBFFT_R2C;
     bool out_real = adjoint ? cfg.type == BBFFT_R2C : cfg.type == BBFFT_C2R;
-    std::size_t const *ist = adjoint ? cfg.ostride : cfg.istride;
-    std::size_t const *ost = adjoint ? cfg.istride : cfg.ostride;
+    stride_t pis = default_istride(dim, shape, cfg.type, false);
+    stride_t pos = default_ostride(dim, shape, cfg.type, false);
+    std::size_t const *ist = strided_nd ? pis.data() : adjoint ? cfg.ostride : cfg.istride;
+    std::size_t const *ost = strided_nd ? pos.data() : adjoint ? cfg.istride : cfg.ostride;
     std::size_t isize = ist[dim + 1] * cfg.shape[dim + 1] * (in_real ? real_b : cplx_b);
     std::size_t osize = ost[dim + 1] * cfg.shape[dim + 1] * (out_real ? real_b : cplx_b);
     if (isize > osize) {
@@ -1477,8 +1490,43 @@ static void make_plan_impl(bbfft_configuration const &cfg, cudaStream_t stream,
     }
     std::size_t n = plan.passes.size();
     for (std::size_t i = 0; i < n; ++i) {
-        plan.passes[i].in_sel = i == 0 ? 0 : 2;
-        plan.passes[i].out_sel = i + 1 == n ? 1 : 2;
+        plan.passes[i].in_sel = i == 0 ? (strided_nd ? 3 : 0) : 2;
+        plan.passes[i].out_sel = i + 1 == n ? (strided_nd ? 4 : 1) : 2;
+    }
+    if (strided_nd) {
+        auto copy_pass = [&](bool gather) {
+            pass cpass;
+            cpass.copy = true;
+            cpass.prec = cfg.precision;
+            copy_params &c = cpass.cp;
+            c.rank = static_cast<int>(dim) + 2;
+            c.gather = gather ? 1 : 0;
+            c.total = 1;
+            bool side_real = gather ? in_real : out_real;
+            bool half = gather ? cfg.type == BBFFT_C2R : cfg.type == BBFFT_R2C;
+            for (unsigned d = 0; d < dim + 2; ++d) {
+                long long e = static_cast<long long>(cfg.shape[d]);
+                if (d == 1 && half) {
+                    e = e / 2 + 1;
+                }
+                c.shape[d] = e;
+                c.stride[d] = static_cast<long long>(gather ? cfg.istride[d] : cfg.ostride[d]);
+                c.total *= e;
+            }
+            std::size_t eb = side_real ? real_b : cplx_b;
+            cpass.func = strided_copy_kernel_ptr(static_cast<int>(eb));
+            cpass.block = 256;
+            long long blocks = (c.total + 255) / 256;
+            cpass.grid = static_cast<unsigned>(std::min<long long>(blocks, 152LL * 16));
+            cpass.in_sel = gather ? 0 : 4;
+            cpass.out_sel = gather ? 3 : 1;
+            cpass.identifier = gather ? "gbfft_strided_gather" : "gbfft_strided_scatter";
+            (gather ? plan.packed_in : plan.packed_out) =
+                std::make_shared<device_buffer>(static_cast<std::size_t>(c.total) * eb);
+            return cpass;
+        };
+        plan.passes.insert(plan.passes.begin(), copy_pass(true));
+        plan.passes.push_back(copy_pass(false));
     }
     plan.inplace_ok = true;
     for (auto const &ps : plan.passes) {
@@ -1496,10 +1544,41 @@ static void execute_impl(bbfft_plan_s &plan, const void *in, void *out, cudaStre
     if (cur != plan.device) {
         GB_CUDA(cudaSetDevice(plan.device));
     }
-    void *tmp = plan.tmp ? plan.tmp->ptr : out;
+    void *packed_in = plan.packed_in ? plan.packed_in->ptr : nullptr;
+    void *packed_out = plan.packed_out ? plan.packed_out->ptr : nullptr;
+    void *tmp = plan.tmp ? plan.tmp->ptr : (packed_out ? packed_out : out);
+    auto select = [&](int sel) -> void * {
+        switch (sel) {
+        case 0:
+            return const_cast<void *>(in);
+        case 1:
+            return out;
+        case 3:
+            return packed_in;
+        case 4:
+            return packed_out;
+        default:
+            return tmp;
+        }
+    };
     for (auto &pass0 : plan.passes) {
-        const void *pin = pass0.in_sel == 0 ? in : tmp;
-        void *pout = pass0.out_sel == 1 ? out : tmp;
+        const void *pin = select(pass0.in_sel);
+        void *pout = select(pass0.out_sel);
+        if (pass0.copy) {
+            copy_params cp = pass0.cp;
+            cp.src = pin;
+            cp.dst = pout;
+            void *cargs[] = {&cp};
+            cudaError_t e = cudaLaunchKernel(pass0.func, dim3(pass0.grid), dim3(pass0.block), cargs, 0, stream);
+            if (e != cudaSuccess) {
+                if (cur != plan.device) {
+                    cudaSetDevice(cur);
+                }
+                throw status_error(BBFFT_CUDA_ERROR,
+                                   std::string("kernel launch failed: ") + cudaGetErrorString(e));
+            }
+            continue;
+        }
         bool misaligned = ((reinterpret_cast<std::uintptr_t>(pin) |
                             reinterpret_cast<std::uintptr_t>(pout)) % 16) != 0;
         if (pass0.tc && misaligned) {
@@ -2179,7 +2258,14 @@ int bbfft_plan_get_info(bbfft_plan_t plan, bbfft_plan_info *info) {
             throw status_error(BBFFT_INVALID_ARGUMENT, "null pointer");
         }
         std::memset(info, 0, sizeof(*info));
-        auto const &ps = plan->passes.front();
+        auto const *first = &plan->passes.front();
+        for (auto const &q : plan->passes) {
+            if (!q.copy) { // the first transform pass (after a strided gather)
+                first = &q;
+                break;
+            }
+        }
+        auto const &ps = *first;
         std::strncpy(info->identifier, ps.identifier.c_str(), sizeof(info->identifier) - 1);
         info->num_launches = static_cast<uint32_t>(plan->passes.size());
         info->inplace_supported = plan->inplace_ok;
@@ -2193,7 +2279,9 @@ int bbfft_plan_get_info(bbfft_plan_t plan, bbfft_plan_info *info) {
         info->kb = static_cast<uint32_t>(ps.p.Kb);
         info->block_threads = ps.block;
         info->shared_bytes = ps.smem;
-        info->workspace_bytes = plan->tmp ? plan->tmp->bytes : 0;
+        info->workspace_bytes = (plan->tmp ? plan->tmp->bytes : 0) +
+                                (plan->packed_in ? plan->packed_in->bytes : 0) +
+                                (plan->packed_out ? plan->packed_out->bytes : 0);
         info->vector_width = static_cast<uint32_t>(ps.V);
         info->specialized = ps.specialized ? 1u : 0u;
         info->min_blocks = static_cast<uint32_t>(ps.min_blocks);

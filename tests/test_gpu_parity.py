@@ -355,3 +355,42 @@ def test_tuned_variants_agree(bb, po, torch_cuda, type, N, M):
                               plan=plan)
                     assert rel_l2(out, ref) <= TOL[4], key
     assert any(k[3] == 3 for k in seen) and any(k[3] == 2 for k in seen)
+
+
+ND_STRIDED = [
+    # dim, shape, type, istride, ostride
+    (2, [1, 8, 8, 2], 0, [1, 1, 9, 80, 0], [1, 1, 9, 80, 0]),           # padded rows
+    (2, [3, 12, 10, 4], 0, [1, 40, 3, 600, 0], [1, 3, 36, 360, 0]),     # transposed N1/N2 input
+    (2, [2, 16, 6, 3], 1, [1, 2, 40, 260, 0], [1, 2, 18, 120, 0]),      # r2c, padded
+    (2, [2, 16, 6, 3], 2, [1, 2, 20, 130, 0], [1, 2, 36, 260, 0]),      # c2r, padded
+    (3, [1, 8, 6, 4, 2], 0, [1, 1, 10, 70, 300], [1, 1, 8, 48, 192]),   # 3d c2c
+]
+
+
+@pytest.mark.parametrize('prec', PRECS)
+@pytest.mark.parametrize('case', ND_STRIDED, ids=[str(c[1]) + str(c[2]) for c in ND_STRIDED])
+def test_nd_custom_layouts(bb, po, torch_cuda, prec, case):
+    """nd transforms with custom strides (a strided gather and scatter around the packed
+    chain), against the FP64 DFT of the gathered tensor."""
+    torch = torch_cuda
+    dim, shape, type, ist, ost = case
+    d = bb.BACKWARD if type == 2 else bb.FORWARD
+    cfg = bb.configuration(dim, shape, precision=prec, type=type, direction=d, istride=ist, ostride=ost)
+    n1in = shape[1] // 2 + 1 if type == 2 else shape[1]
+    n1out = shape[1] // 2 + 1 if type == 1 else shape[1]
+    ishape = [shape[0], n1in] + shape[2:dim + 2]
+    oshape = [shape[0], n1out] + shape[2:dim + 2]
+    isize = po.tensor_size(dim, ishape, ist)
+    osize = po.tensor_size(dim, oshape, ost)
+    rdt, cdt = dtypes(prec)
+    rng = np.random.default_rng(sum(shape) + type)
+    if type == 1:
+        x = rng.standard_normal(isize).astype(rdt)
+    else:
+        x = (rng.standard_normal(isize) + 1j * rng.standard_normal(isize)).astype(cdt)
+    out = run(bb, torch, cfg, x, osize, rdt if type == 2 else cdt)
+    ref = po.dft64(dim, shape, type, d, po.gather(x.astype(np.float64 if type == 1 else np.complex128), dim, ishape, ist))
+    got = po.gather(out, dim, oshape, ost)
+    assert rel_l2(got, ref) <= TOL[prec]
+    info = bb.Plan(cfg, stream=torch.cuda.current_stream().cuda_stream).info()
+    assert info.num_launches == dim + 2 and info.workspace_bytes > 0
