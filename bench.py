@@ -305,6 +305,7 @@ def run_ours(args):
         legs['ragged_10k'] = leg_ragged(bb, torch, stream, hbm_peak, args.steps, args.warmup)
         legs['spectral_layer_2d'] = leg_spectral(bb, torch, stream, args.steps, args.warmup)
         legs['c2c_3d_64'] = leg_c2c_3d(bb, torch, stream, hbm_peak, args.steps, args.warmup)
+        legs['tft_vs_double_batched'] = leg_tft(bb, torch, stream, hbm_peak, args.steps, args.warmup)
         legs['sweep_f64'] = leg_sweep_f64(bb, torch, stream, hbm_peak, max(2, args.steps // 2), 1)
         torch.cuda.empty_cache()
         legs['tensor_core_c2c'] = leg_tensor_core(bb, torch, stream, hbm_peak, args.steps, args.warmup)
@@ -484,6 +485,39 @@ def leg_spectral(bb, torch, stream, steps, warmup):
         step()
     ms = event_time(torch, stream, step, max(steps, 3))
     return {'ms_fwd_bwd': round(ms, 3), 'shape': 'r2c/c2r 128x128, K=2048, modes 32x32, f32'}
+
+
+def leg_tft(bb, torch, stream, hbm_peak, steps, warmup):
+    """The reference's transpose-FFT-transpose example (examples/transpose_fft_transpose):
+    c2c float over the N mode of an M x N x K tensor (M = 64, N = 64, 512 MB), either as
+    transpose -> contiguous FFT (M = 1) -> transpose, or as one double-batched plan that
+    reads the M x N x K layout directly (the transposes folded into its loads and stores)."""
+    sptr = stream.cuda_stream
+    M, N = 64, 64
+    K = (512 * 1000 * 1000) // (8 * M * N)
+    x = torch.randn(K, N, M, dtype=torch.complex64, device='cuda')
+    y = torch.empty_like(x)
+    direct = bb.Plan(bb.configuration(1, [M, N, K], precision=bb.F32), stream=sptr)
+    inner = bb.Plan(bb.configuration(1, [1, N, M * K], precision=bb.F32), stream=sptr)
+    xt = torch.empty(K, M, N, dtype=torch.complex64, device='cuda')
+
+    def tft():
+        xt.copy_(x.permute(0, 2, 1))                      # (K, M, N): N contiguous
+        inner.execute(xt.data_ptr())                      # in place, M = 1
+        y.copy_(xt.permute(0, 2, 1))                      # back to (K, N, M)
+
+    def dbl():
+        direct.execute(x.data_ptr(), y.data_ptr())
+
+    for _ in range(warmup):
+        tft()
+        dbl()
+    ms_tft = event_time(torch, stream, tft, max(steps, 3))
+    ms_dbl = event_time(torch, stream, dbl, max(steps, 3))
+    b = 2 * M * N * K * 8
+    return {'ms_transpose_fft_transpose': round(ms_tft, 3), 'ms_double_batched': round(ms_dbl, 3),
+            'gbs_double_batched': round(b / ms_dbl / 1e6, 1), 'speedup': round(ms_tft / ms_dbl, 2),
+            'shape': 'c2c f32 M=64 N=64 K=%d' % K}
 
 
 def leg_c2c_3d(bb, torch, stream, hbm_peak, steps, warmup):

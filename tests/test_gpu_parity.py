@@ -394,3 +394,19 @@ def test_nd_custom_layouts(bb, po, torch_cuda, prec, case):
     assert rel_l2(got, ref) <= TOL[prec]
     info = bb.Plan(cfg, stream=torch.cuda.current_stream().cuda_stream).info()
     assert info.num_launches == dim + 2 and info.workspace_bytes > 0
+
+
+def test_transpose_fft_transpose_equals_double_batched(bb, torch_cuda):
+    """reference examples/transpose_fft_transpose: transpose -> FFT over contiguous N ->
+    transpose equals one double-batched plan over the M x N x K layout."""
+    torch = torch_cuda
+    M, N, K = 16, 64, 40
+    s = torch.cuda.current_stream().cuda_stream
+    x = torch.randn(K, N, M, dtype=torch.complex64, device='cuda')
+    y = torch.empty_like(x)
+    bb.Plan(bb.configuration(1, [M, N, K], precision=bb.F32), stream=s).execute(x.data_ptr(), y.data_ptr())
+    xt = x.permute(0, 2, 1).contiguous()
+    bb.Plan(bb.configuration(1, [1, N, M * K], precision=bb.F32), stream=s).execute(xt.data_ptr())
+    torch.cuda.synchronize()
+    y2 = xt.permute(0, 2, 1)
+    assert float(torch.linalg.vector_norm(y - y2) / torch.linalg.vector_norm(y2)) <= 1e-6
