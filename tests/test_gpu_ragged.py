@@ -103,3 +103,51 @@ def test_ragged_rejects_mixed_precision(bb, torch_cuda):
              (bb.F64, bb.FORWARD, bb.C2C, 16, 1, 1, a.data_ptr(), a.data_ptr() + 512)]
     with pytest.raises(bb.BadConfiguration):
         bb.Ragged(items)
+
+
+@pytest.mark.parametrize('prec', [4, 8])
+@pytest.mark.parametrize('form', [0, 1, 2])
+def test_ragged_every_kind(bb, po, torch_cuda, prec, form):
+    """c2c forward and backward, r2c and c2r items, even and odd N, in one batch of each
+    precision and launch form, against the FP64 DFT (the reference's c2r semantics)."""
+    torch = torch_cuda
+    rng = np.random.default_rng(31 + prec + form)
+    rdt, cdt = (np.float32, np.complex64) if prec == 4 else (np.float64, np.complex128)
+    specs, xs = [], []
+    in_off = out_off = 0
+    for i in range(120):
+        N = int(rng.choice([7, 12, 16, 40, 61, 96, 136, 250, 488, 512]))
+        t = int(rng.choice([bb.C2C, bb.R2C, bb.C2R]))
+        d = bb.BACKWARD if t == bb.C2R else (int(rng.choice([bb.FORWARD, bb.BACKWARD])) if t == bb.C2C else bb.FORWARD)
+        M = int(rng.choice([1, 3, 8]))
+        K = int(rng.integers(1, 12))
+        nin = N // 2 + 1 if t == bb.C2R else N
+        nout = N // 2 + 1 if t == bb.R2C else N
+        if t == bb.R2C:
+            x = rng.standard_normal(M * nin * K).astype(rdt)
+        else:
+            x = (rng.standard_normal(M * nin * K) + 1j * rng.standard_normal(M * nin * K)).astype(cdt)
+        ib = x.nbytes
+        ob = M * nout * K * (np.dtype(rdt).itemsize if t == bb.C2R else np.dtype(cdt).itemsize)
+        specs.append((t, d, N, M, K, in_off, out_off, x, nout))
+        in_off += (ib + 15) // 16 * 16
+        out_off += (ob + 15) // 16 * 16
+    xin = torch.zeros(in_off, dtype=torch.uint8, device='cuda')
+    yout = torch.zeros(out_off, dtype=torch.uint8, device='cuda')
+    for (t, d, N, M, K, io, oo, x, nout) in specs:
+        raw = torch.from_numpy(x.view(np.uint8).copy())
+        xin[io:io + raw.numel()].copy_(raw)
+    items = [(prec, d, t, N, M, K, xin.data_ptr() + io, yout.data_ptr() + oo)
+             for (t, d, N, M, K, io, oo, x, nout) in specs]
+    r = bb.Ragged(items)
+    r.set_launch_form(form)
+    r.execute(torch.cuda.current_stream().cuda_stream, use_graph=True)
+    torch.cuda.synchronize()
+    yh = yout.cpu().numpy()
+    for (t, d, N, M, K, io, oo, x, nout) in specs:
+        odt = rdt if t == bb.C2R else cdt
+        got = yh[oo:oo + M * nout * K * np.dtype(odt).itemsize].view(odt)
+        nin = N // 2 + 1 if t == bb.C2R else N
+        ref = po.dft64(1, [M, N, K], t, d, x.astype(np.float64 if t == bb.R2C else np.complex128).reshape(K, nin, M))
+        e = rel_l2(got.reshape(ref.shape), ref)
+        assert e <= TOL[prec], (t, d, N, M, K, e)
