@@ -115,8 +115,10 @@ def vector_width(prec, rad):
 # over T threads runs ceil(nb / T) rounds.
 ALT_STAGES = {
     80: [([10, 8], 10), ([8, 10], 8), ([8, 10], 10), ([16, 5], 5), ([5, 16], 5)],
-    112: [([16, 7], 16), ([7, 16], 7), ([7, 16], 16), ([4, 4, 7], 28)],
-    192: [([8, 6, 4], 32), ([16, 12], 12), ([12, 16], 12), ([16, 12], 16), ([4, 6, 8], 48)],
+    112: [([16, 7], 16), ([7, 16], 7), ([7, 16], 16), ([4, 4, 7], 28), ([7, 16], 32),
+          ([4, 4, 7], 16), ([16, 7], 8)],
+    192: [([8, 6, 4], 32), ([16, 12], 12), ([12, 16], 12), ([16, 12], 16), ([4, 6, 8], 48),
+          ([16, 12], 24), ([12, 16], 24), ([8, 8, 3], 24), ([3, 8, 8], 24)],
 }
 
 
