@@ -118,7 +118,8 @@ ALT_STAGES = {
     112: [([16, 7], 16), ([7, 16], 7), ([7, 16], 16), ([4, 4, 7], 28), ([7, 16], 32),
           ([4, 4, 7], 16), ([16, 7], 8)],
     192: [([8, 6, 4], 32), ([16, 12], 12), ([12, 16], 12), ([16, 12], 16), ([4, 6, 8], 48),
-          ([16, 12], 24), ([12, 16], 24), ([8, 8, 3], 24), ([3, 8, 8], 24)],
+          ([16, 12], 24), ([12, 16], 24), ([8, 8, 3], 24), ([3, 8, 8], 24),
+          ([12, 4, 4], 16), ([4, 4, 12], 16), ([16, 12], 8), ([12, 16], 8), ([8, 6, 4], 8)],
 }
 
 
