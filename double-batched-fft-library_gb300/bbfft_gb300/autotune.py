@@ -45,7 +45,9 @@ def tune_config(torch, prec, type, N, M, K, reps=4, verbose=False):
         occs += (12, 13)  # paired c2r pre-process variants
     stages = [(None, 0)]
     if prec == 4 and type != bb.C2C and N % 2 == 0:
-        stages += [(tuple(r), t) for r, t in alt_stages().get(N // 2, [])]
+        stages += [(tuple(r), t) for r, t in alt_stages()[0].get(N // 2, [])]
+    if prec == 4 and type == bb.C2C:
+        stages += [(tuple(r), t) for r, t in alt_stages()[1].get(N, [])]
     for rad, T in stages:
      for V in (0, 1, 2, 4):
         for Mb in mbs:
@@ -115,14 +117,14 @@ def default_configs(quick=False):
 
 
 def alt_stages():
-    """Alternative (radices, threads per transform) with compile-time kernels, by half length
-    (csrc/gen_specializations.py ALT_STAGES)."""
+    """Alternative (radices, threads per transform) with compile-time kernels: by real half
+    length and by c2c length (csrc/gen_specializations.py ALT_STAGES, ALT_STAGES_C2C)."""
     csrc = os.path.join(os.path.dirname(HERE), 'csrc')
     if csrc not in sys.path:
         sys.path.insert(0, csrc)
     import gen_specializations
 
-    return gen_specializations.ALT_STAGES
+    return gen_specializations.ALT_STAGES, gen_specializations.ALT_STAGES_C2C
 
 
 def read_table(path):

@@ -123,6 +123,12 @@ ALT_STAGES = {
 }
 
 
+# the same for float c2c lengths
+ALT_STAGES_C2C = {
+    512: [([16, 8, 4], 32), ([8, 8, 8], 32), ([16, 16, 2], 32), ([4, 8, 16], 32), ([8, 8, 8], 16)],
+}
+
+
 def entries():
     out = []
     for prec in (4, 8):
@@ -135,6 +141,8 @@ def entries():
                 variants = [(rad, T)]
                 if prec == 4 and kind in (1, 3):
                     variants += ALT_STAGES.get(nc, [])
+                if prec == 4 and kind == 0:
+                    variants += ALT_STAGES_C2C.get(nc, [])
                 for rad, T in variants:
                     for V in sorted({1, vector_width(prec, rad)}):
                         # kernel variant: resident CTAs the register allocation is sized for,
