@@ -1724,8 +1724,24 @@ static void make_ragged(bbfft_ragged_item const *items, std::size_t n, bbfft_rag
             units.push_back({cost, {static_cast<int>(i), static_cast<int>(t)}});
         }
     }
-    std::stable_sort(units.begin(), units.end(),
-                     [](auto const &a, auto const &b) { return a.first > b.first; });
+    // order: classes of units with the same tile function together (the CTAs running at the
+    // same time then execute the same code, which keeps the instruction cache warm), the
+    // class with the most work first, largest tiles first inside a class
+    {
+        auto key_of = [&](int i) { return dev[i].vid >= 0 ? dev[i].vid : -1 - (r.prec * 8 + dev[i].kind); };
+        std::map<int, double> class_cost;
+        for (auto const &u : units) {
+            class_cost[key_of(u.second.first)] += u.first;
+        }
+        std::stable_sort(units.begin(), units.end(), [&](auto const &a, auto const &b) {
+            int ka = key_of(a.second.first), kb = key_of(b.second.first);
+            if (ka != kb) {
+                double ca = class_cost[ka], cb = class_cost[kb];
+                return ca != cb ? ca > cb : ka < kb;
+            }
+            return a.first > b.first;
+        });
+    }
     // class form: units grouped by tile function, LPT order kept inside a class
     {
         std::map<int, std::vector<int>> by_class; // key: vid, or -1 - (prec * 8 + kind)
