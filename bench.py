@@ -10,8 +10,9 @@ value  = algorithmic bytes of all passes / device time of the step (GB/s), where
          moves (N * 4 + (N/2+1) * 8) * M * K bytes (one read + one write, the reference's
          benchmark/adapter.hpp:21-25,51-52 byte model); inputs are resident in HBM and are
          1 GiB per pass, far larger than the 129 MB L2, so no flush is needed.
-e2e    = the same metric through the C ABI with pinned host buffers: each step copies the
-         inputs host->device, runs the passes and copies the results device->host.
+e2e    = the same metric through the C ABI from pinned host memory (1/8 of K per N): each
+         step copies the inputs host->device, runs the passes and copies the results
+         device->host, in K-chunks pipelined over two copy streams and a compute stream.
 roofline = the engine kernels (every launch of the step): algorithmic bytes / summed
          CUDA-event duration of the launches, against the measured HBM copy bandwidth.
 cpu_baseline = the oracle (C restatement of the reference's algorithm) on all host cores,
