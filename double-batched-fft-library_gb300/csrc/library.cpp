@@ -1744,19 +1744,16 @@ static void make_ragged(bbfft_ragged_item const *items, std::size_t n, bbfft_rag
     }
     // class form: units grouped by tile function, LPT order kept inside a class
     {
-        // key: (vid, or -1 - (prec * 8 + kind) for the runtime engine; threads of the tile
-        // rounded to a warp), so that every kernel's CTAs are as large as its tiles
-        std::map<std::pair<int, int>, std::vector<int>> by_class;
+        std::map<int, std::vector<int>> by_class; // key: vid, or -1 - (prec * 8 + kind)
         for (std::size_t u = 0; u < units.size(); ++u) {
             int i = units[u].second.first;
             int key = dev[i].vid >= 0 ? dev[i].vid : -1 - (r.prec * 8 + dev[i].kind);
-            int threads = static_cast<int>((r.passes[i].block + 31) / 32 * 32);
-            by_class[{key, threads}].push_back(static_cast<int>(u));
+            by_class[key].push_back(static_cast<int>(u));
         }
         std::vector<int> cflat;
         for (auto const &kv : by_class) {
             bbfft_ragged_s::unit_class c{};
-            c.func = kv.first.first >= 0 ? ragged_class_kernel(kv.first.first)
+            c.func = kv.first >= 0 ? ragged_class_kernel(kv.first)
                                    : ragged_class_runtime_kernel(r.prec, dev[units[kv.second[0]].second.first].kind);
             if (!c.func) {
                 throw status_error(BBFFT_INTERNAL_ERROR, "ragged class kernel not found");
