@@ -158,7 +158,7 @@ def entries():
 
 # Ragged batches: float c2c N = 16..512 step 8 and r2c N = 16..512 step 8 (half length
 # 8..256 step 4), one thread per M (V = 1), as device functions of the persistent kernel.
-RAGGED_FILES = 6
+RAGGED_FILES = 8
 
 
 def ragged_entries():
@@ -169,6 +169,11 @@ def ragged_entries():
             if any(r not in UNROLLED and r not in BIG_PRIMES for r in rad):
                 continue
             out.append((4, kind, nc, T, rad, 1))
+            # vectorised over M (items with M a multiple of V and 16-byte aligned tensors);
+            # the prime stages are scalar
+            vw = vector_width(4, rad)
+            if vw > 1 and not any(r in BIG_PRIMES for r in rad):
+                out.append((4, kind, nc, T, rad, vw))
     return out
 
 

@@ -972,10 +972,22 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     // ragged batches, and plans of lengths without a compile-time plan kernel
     int ragged_vid = -1;
     if (!has_cb && !ct && q.prec == 4) {
-        ragged_vid = ragged_ct_lookup(q.prec, ps.kind, Nc, T, 1, rad.data(), L);
+        int vw = vector_width(q.prec, rad);
+        if (reqV > 0) {
+            vw = std::min(vw, reqV);
+        }
+        bool v_ok = !q.force_v1 && vw > 1 && M % vw == 0 && q.is1 % vw == 0 && q.os1 % vw == 0 &&
+                    q.is2 % vw == 0 && q.os2 % vw == 0;
+        if (v_ok) {
+            ragged_vid = ragged_ct_lookup(q.prec, ps.kind, Nc, T, vw, rad.data(), L);
+            V = ragged_vid >= 0 ? vw : 1;
+        }
+        if (ragged_vid < 0) {
+            ragged_vid = ragged_ct_lookup(q.prec, ps.kind, Nc, T, 1, rad.data(), L);
+            V = 1;
+        }
         if (ragged_vid >= 0) {
             ct = &ragged_ct_table[ragged_vid];
-            V = 1;
         }
     }
     int const max_block = q.max_block > 0 ? q.max_block : (ct ? 256 : 512);
@@ -1702,7 +1714,8 @@ static void make_ragged(bbfft_ragged_item const *items, std::size_t n, bbfft_rag
         q.os2 = q.M * nout;
         q.runtime_only = true;
         q.max_block = block;
-        q.force_v1 = true;
+        // tiles vectorised over M need 16-byte aligned tensors
+        q.force_v1 = ((reinterpret_cast<std::uintptr_t>(it.in) | reinterpret_cast<std::uintptr_t>(it.out)) % 16) != 0;
         r.passes.push_back(make_1d_pass(q, r.device, nullptr));
         pass const &ps = r.passes.back();
         dev[i].p = ps.p;
