@@ -497,6 +497,11 @@ static int max_optin_smem(int device) {
 // The dynamic shared-memory limit is a property of the kernel, shared by every plan that
 // launches it: raise it once per kernel and device to the device maximum (lowering it for
 // one plan would break the launches of another).
+// Whether `smem` dynamic bytes need the opt-in limit: the default limit is 48 KiB minus the
+// kernel's static shared memory (1 KiB of margin covers the library's kernels, whose static
+// shared memory is a parameter block of a few hundred bytes).
+static bool needs_smem_optin(std::size_t smem) { return smem > 47 * 1024; }
+
 // Raise a kernel's dynamic shared-memory limit to the device maximum.  Kernels compiled
 // into the library are set once per device; kernels of NVRTC modules (module_kernel) are
 // set every time, since a handle of an unloaded module can be reused by a new one.
@@ -1159,7 +1164,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         ps.mod = mod;
         ps.func = reinterpret_cast<const void *>(k);
     }
-    if (smem > 48 * 1024) {
+    if (needs_smem_optin(smem)) {
         allow_max_smem(ps.func, device, static_cast<bool>(ps.mod));
     }
     return ps;
@@ -1783,7 +1788,7 @@ static void make_ragged(bbfft_ragged_item const *items, std::size_t n, bbfft_rag
                 cflat.push_back(units[u].second.first);
                 cflat.push_back(units[u].second.second);
             }
-            if (c.smem > 48 * 1024) {
+            if (needs_smem_optin(c.smem)) {
                 allow_max_smem(c.func, r.device);
             }
             r.classes.push_back(c);
@@ -1809,7 +1814,7 @@ static void make_ragged(bbfft_ragged_item const *items, std::size_t n, bbfft_rag
     r.grid_func = ragged_kernel_ptr(r.prec, false);
     r.block = block;
     r.smem = smem;
-    if (smem > 48 * 1024) {
+    if (needs_smem_optin(smem)) {
         allow_max_smem(r.func, r.device);
         allow_max_smem(r.grid_func, r.device);
     }
@@ -1844,8 +1849,20 @@ static void launch_ragged(bbfft_ragged_s &r, cudaStream_t stream) {
         for (auto const &c : r.classes) {
             const void *cu = static_cast<const int2 *>(r.class_units->ptr) + c.offset;
             void *cargs[] = {&items, &cu};
-            GB_CUDA(cudaLaunchKernel(c.func, dim3(static_cast<unsigned>(c.count)), dim3(c.block),
-                                     cargs, c.smem, stream));
+            cudaError_t e = cudaLaunchKernel(c.func, dim3(static_cast<unsigned>(c.count)),
+                                             dim3(c.block), cargs, c.smem, stream);
+            if (e != cudaSuccess) {
+                (void)cudaGetLastError();
+                cudaFuncAttributes fa = {};
+                cudaFuncGetAttributes(&fa, c.func);
+                throw status_error(BBFFT_CUDA_ERROR,
+                                   std::string("ragged class launch failed: ") + cudaGetErrorString(e) +
+                                       " (block " + std::to_string(c.block) + ", dynamic shared " +
+                                       std::to_string(c.smem) + " B, max dynamic " +
+                                       std::to_string(fa.maxDynamicSharedSizeBytes) + " B, max threads " +
+                                       std::to_string(fa.maxThreadsPerBlock) + ", registers " +
+                                       std::to_string(fa.numRegs) + ")");
+            }
         }
         return;
     }
