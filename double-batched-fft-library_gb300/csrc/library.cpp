@@ -1645,7 +1645,8 @@ struct bbfft_ragged_s {
     const void *func = nullptr;      // persistent kernel
     const void *grid_func = nullptr; // one CTA per unit
     int form = BBFFT_RAGGED_PERSISTENT;
-    // class form: one kernel per class of units (same tile function), independent graph nodes
+    // class form: one kernel per class of units (same tile function); as a graph, the
+    // kernels form four chains of nodes
     struct unit_class {
         const void *func;
         int offset, count; // units class_units[offset, offset + count)
