@@ -5,7 +5,7 @@ aot_cache at run time).
     python -m bbfft_gb300.aot -o kernels.cubin --callbacks user.cu [--load NAME] [--store NAME]
                               [--arch sm_103a] DESCRIPTOR...
 
-compiles the kernels that the 1d configurations DESCRIPTOR... (reference descriptor
+compiles the kernels that the configurations DESCRIPTOR... (reference descriptor
 strings, e.g. ``scfo64*1000``) need with the user module of ``--callbacks`` into one cubin
 ``kernels.cubin`` and writes their names to ``kernels.cubin.names``.  ``--arch`` compiles
 for that architecture without a GPU (BBFFT_GB300_AOT_ARCH).  Kernels of configurations

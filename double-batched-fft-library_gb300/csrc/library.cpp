@@ -764,40 +764,57 @@ std::string callback_kernel_name(int prec, int kind, const char *src, std::size_
     return c_ident(key.str());
 }
 
-// NVRTC program: the engine, the user module and one kernel per (name, precision, kind).
-// The user's load / store functions are called with the element offset of the tensor
-// (reference callback_accessor, src/base/generator/tensor_accessor.cpp:34-55).
+// NVRTC program: the engine, the user module and one kernel per (name, precision, kind,
+// io).  io selects which of the user's functions the kernel calls (bit 0: load, bit 1:
+// store); the passes of an nd plan call the load function in the first pass only and the
+// store function in the last pass only.  The user's load / store functions are called with
+// the element offset of the tensor (reference callback_accessor,
+// src/base/generator/tensor_accessor.cpp:34-55).
 std::string callback_program(const char *cb, std::size_t len, const char *load_fn,
                              const char *store_fn,
-                             std::vector<std::tuple<std::string, int, int>> const &kernels) {
+                             std::vector<std::tuple<std::string, int, int, int>> const &kernels) {
     std::ostringstream src;
     src << "typedef decltype(sizeof(0)) size_t;\n";
     src << kEngineSource << "\n";
     src << std::string(cb, len) << "\n";
-    src << "struct gbfft_user_io {\n"
-        << "  static constexpr bool direct = false;\n"
-        << "  template <class T> static __device__ __forceinline__ T load(const T *t, long long "
-           "base, int off) {\n";
-    if (load_fn && *load_fn) {
-        src << "    return " << load_fn << "(const_cast<T *>(t), (size_t)(base + off));\n";
-    } else {
-        src << "    return (t + base)[off];\n";
+    std::set<int> ios;
+    for (auto const &k : kernels) {
+        ios.insert(std::get<3>(k));
     }
-    src << "  }\n  template <class T> static __device__ __forceinline__ void store(T *t, long long "
-           "base, int off, T v) {\n";
-    if (store_fn && *store_fn) {
-        src << "    " << store_fn << "(t, (size_t)(base + off), v);\n";
-    } else {
-        src << "    (t + base)[off] = v;\n";
+    for (int io : ios) {
+        bool user_load = (io & 1) && load_fn && *load_fn;
+        bool user_store = (io & 2) && store_fn && *store_fn;
+        src << "struct gbfft_user_io_" << io << " {\n"
+            << "  static constexpr bool direct = false;\n"
+            << "  template <class T> static __device__ __forceinline__ T load(const T *t, long long "
+               "base, int off) {\n";
+        if (user_load) {
+            src << "    return " << load_fn << "(const_cast<T *>(t), (size_t)(base + off));\n";
+        } else {
+            src << "    return (t + base)[off];\n";
+        }
+        src << "  }\n  template <class T> static __device__ __forceinline__ void store(T *t, long long "
+               "base, int off, T v) {\n";
+        if (user_store) {
+            src << "    " << store_fn << "(t, (size_t)(base + off), v);\n";
+        } else {
+            src << "    (t + base)[off] = v;\n";
+        }
+        src << "  }\n};\n";
     }
-    src << "  }\n};\n";
     for (auto const &k : kernels) {
         src << "extern \"C\" __global__ void __launch_bounds__(512) " << std::get<0>(k)
             << "(const __grid_constant__ gbfft::fft_params p) {\n"
             << "  gbfft::fft_tile<" << (std::get<1>(k) == 4 ? "float" : "double") << ", "
-            << std::get<2>(k) << ", gbfft_user_io>(p);\n}\n";
+            << std::get<2>(k) << ", gbfft_user_io_" << std::get<3>(k) << ">(p);\n}\n";
     }
     return src.str();
+}
+
+// Which user functions a pass with these load / store names calls (the io of
+// callback_program).
+int callback_io(const char *load_fn, const char *store_fn) {
+    return ((load_fn && *load_fn) ? 1 : 0) | ((store_fn && *store_fn) ? 2 : 0);
 }
 
 pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
@@ -1150,8 +1167,9 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
             mod = cache->get(kname, device);
         }
         if (!mod) {
-            std::string src = callback_program(q.cb_source, q.cb_length, q.load_fn, q.store_fn,
-                                               {std::make_tuple(kname, q.prec, ps.kind)});
+            std::string src = callback_program(
+                q.cb_source, q.cb_length, q.load_fn, q.store_fn,
+                {std::make_tuple(kname, q.prec, ps.kind, callback_io(q.load_fn, q.store_fn))});
             mod = nvrtc_build(src, kname, device);
             if (cache) {
                 cache->store(kname, device, mod);
@@ -1386,12 +1404,12 @@ static void make_plan_impl(bbfft_configuration const &cfg, cudaStream_t stream,
     // such layouts, src/common/algorithm/nd_fft.hpp:47-49)
     bool strided_nd = false;
     if (cfg.dim > 1) {
-        if (has_cb) {
-            bad_config("User modules are unsuported for FFT dimension > 1.");
-        }
         if (!is_default(false) && !is_default(true)) {
             if (adjoint) {
                 bad_config("adjoint plans of nd transforms need a default tensor layout");
+            }
+            if (has_cb) {
+                bad_config("callbacks of nd transforms need a default tensor layout");
             }
             strided_nd = true;
         }
@@ -1489,9 +1507,21 @@ static void make_plan_impl(bbfft_configuration const &cfg, cudaStream_t stream,
             std::swap(q.is2, q.os2);
         }
     }
-    for (auto &q : order) {
+    // user callbacks (the reference takes none for dim > 1, nd_fft.hpp:29-31): the first
+    // pass reads the input tensor in its own layout and the last pass writes the output
+    // tensor in its own layout, so the load function runs in the first pass and the store
+    // function in the last, each with the element offset of its tensor
+    for (std::size_t i = 0; i < order.size(); ++i) {
+        pass_request &q = order[i];
+        if (has_cb) {
+            q.cb_source = cfg.callback_source;
+            q.cb_length = cfg.callback_length;
+            q.load_fn = i == 0 ? cfg.load_function : nullptr;
+            q.store_fn = i + 1 == order.size() ? cfg.store_function : nullptr;
+        }
         plan.passes.push_back(make_1d_pass(q, plan.device, cache));
     }
+    plan.jit = has_cb;
     // temporary buffer if the input is larger than the output (nd_fft.hpp:114-125)
     std::size_t real_b = cfg.precision, cplx_b = 2 * real_b;
     bool in_real = adjoint ? cfg.type == BBFFT_C2R : cfg.type == BBFFT_R2C;
@@ -1999,16 +2029,16 @@ int bbfft_aot_generate(const bbfft_configuration *cfgs, size_t num_cfgs, void *i
             throw status_error(BBFFT_INVALID_ARGUMENT, "no configurations");
         }
         const bbfft_configuration &c0 = cfgs[0];
-        std::vector<std::tuple<std::string, int, int>> kernels;
+        std::vector<std::tuple<std::string, int, int, int>> kernels;
         std::set<std::string> seen;
         for (size_t i = 0; i < num_cfgs; ++i) {
             const bbfft_configuration &c = cfgs[i];
             gbfft::validate(c);
             bool has_cb = (c.load_function && *c.load_function) ||
                           (c.store_function && *c.store_function);
-            if (!has_cb || c.dim != 1) {
+            if (!has_cb) {
                 throw status_error(BBFFT_BAD_CONFIGURATION,
-                                   "only 1d configurations with callbacks need generated "
+                                   "only configurations with callbacks need generated "
                                    "kernels; the others are built into the library");
             }
             if (c.callback_length != c0.callback_length ||
@@ -2025,11 +2055,25 @@ int bbfft_aot_generate(const bbfft_configuration *cfgs, size_t num_cfgs, void *i
                        : c.type == BBFFT_R2C
                            ? (even ? gbfft::kind_r2c_half : gbfft::kind_r2c_full)
                            : (even ? gbfft::kind_c2r_half : gbfft::kind_c2r_full);
-            std::string name = gbfft::callback_kernel_name(c.precision, kind, c.callback_source,
-                                                           c.callback_length, c.load_function,
-                                                           c.store_function);
-            if (seen.insert(name).second) {
-                kernels.emplace_back(name, c.precision, kind);
+            auto add = [&](int k, const char *load_fn, const char *store_fn) {
+                if (gbfft::callback_io(load_fn, store_fn) == 0) {
+                    return;
+                }
+                std::string name = gbfft::callback_kernel_name(
+                    c.precision, k, c.callback_source, c.callback_length, load_fn, store_fn);
+                if (seen.insert(name).second) {
+                    kernels.emplace_back(name, c.precision, k,
+                                         gbfft::callback_io(load_fn, store_fn));
+                }
+            };
+            if (c.dim == 1) {
+                add(kind, c.load_function, c.store_function);
+            } else {
+                // the passes of an nd plan that call user functions: the first (load) and
+                // the last (store); c2r runs the outer modes first and its real pass last
+                bool c2r = c.type == BBFFT_C2R;
+                add(c2r ? gbfft::kind_c2c : kind, c.load_function, nullptr);
+                add(c2r ? kind : gbfft::kind_c2c, nullptr, c.store_function);
             }
         }
         // the current device's architecture, or BBFFT_GB300_AOT_ARCH when it is set (also

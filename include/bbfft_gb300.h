@@ -79,6 +79,10 @@ typedef enum bbfft_status {
  *   T load(const T* in, size_t offset)          -- T = float2/double2 or float/double
  *   void store(T* out, size_t offset, T value)
  * compiled for sm_103a with NVRTC at plan creation (the reference compiles OpenCL-C).
+ * offset counts elements of the input (load) or output (store) tensor.  For dim > 1 (the
+ * reference rejects callbacks there, src/common/algorithm/nd_fft.hpp:29-31) the tensors
+ * need one of the default layouts: load is called for every element read from the input
+ * tensor, store for every element written to the output tensor.
  */
 typedef struct bbfft_configuration {
     uint32_t dim;                             /* 1..3 */
@@ -132,7 +136,7 @@ BBFFT_GB300_API int bbfft_aot_cache_register_module(bbfft_cache_t cache, const v
                                                     const char *const *kernel_names,
                                                     size_t num_kernel_names, int device);
 /* reference: bbfft-aot-generate (tools/aot/main.cpp:22-60) over generate_fft_kernels
- * (src/base/generator.cpp:16-25).  Compiles the kernels that 1d configurations with user
+ * (src/base/generator.cpp:16-25).  Compiles the kernels that configurations with user
  * callbacks need (all sharing one user module) into one cubin for the current device (or,
  * when the environment variable BBFFT_GB300_AOT_ARCH names one, e.g. sm_103a, for that
  * architecture without touching a GPU), to be registered with

@@ -109,10 +109,13 @@ def test_unsupported_dimension_is_bad_configuration(bb, dim):
         bb.make_plan(cfg)
 
 
-def test_callbacks_rejected_for_nd(bb):
-    """reference src/common/algorithm/nd_fft.hpp:29-31"""
-    cfg = bb.configuration(2, [1, 8, 8, 1], callbacks=('x', 'load', None))
-    with pytest.raises(bb.BadConfiguration, match='User modules'):
+def test_nd_callbacks_need_default_layout(bb):
+    """nd callbacks (the reference rejects them, src/common/algorithm/nd_fft.hpp:29-31) run in
+    the first and last pass of the chain; custom nd layouts, whose chain runs on packed
+    copies, cannot take them"""
+    cfg = bb.configuration(2, [1, 8, 8, 2], istride=[1, 1, 9, 80, 0], ostride=[1, 1, 9, 80, 0],
+                           callbacks=('x', 'load', None))
+    with pytest.raises(bb.BadConfiguration, match='callbacks of nd transforms'):
         bb.make_plan(cfg)
 
 

@@ -184,3 +184,91 @@ def test_aot_tool_image_serves_plans(bb, torch_cuda, tmp_path):
     y_aot = run(bb, torch, cfg, X, 4 * 64 * 8, np.float32, plan=p_aot)
     y_jit = run(bb, torch, cfg, X, 4 * 64 * 8, np.float32)
     assert np.array_equal(y_aot, y_jit)
+
+
+ND_SRC = """
+{T2} load_w({T2} *in, size_t offset) {{
+    {T2} v = in[offset];
+    {T} w = ({T})1 + ({T})(offset % 5) * ({T})0.25;
+    v.x = v.x * w;
+    v.y = v.y * w;
+    return v;
+}}
+{T} load_w({T} *in, size_t offset) {{
+    return in[offset] * (({T})1 + ({T})(offset % 5) * ({T})0.25);
+}}
+void store_w({T2} *out, size_t offset, {T2} v) {{
+    {T} w = ({T})1 + ({T})(offset % 3) * ({T})0.5;
+    v.x = v.x * w;
+    v.y = v.y * w;
+    out[offset] = v;
+}}
+void store_w({T} *out, size_t offset, {T} v) {{
+    out[offset] = v * (({T})1 + ({T})(offset % 3) * ({T})0.5);
+}}
+"""
+
+ND_CASES = [
+    # dim, shape, type, inplace
+    (2, [2, 8, 6, 3], 0, False),
+    (2, [1, 12, 10, 2], 0, True),
+    (2, [2, 16, 6, 3], 1, False),
+    (2, [3, 10, 4, 2], 1, True),
+    (2, [2, 16, 6, 3], 2, False),
+    (2, [1, 12, 5, 2], 2, True),
+    (3, [1, 8, 6, 4, 2], 0, False),
+    (3, [2, 8, 4, 6, 2], 1, False),
+    (3, [1, 6, 4, 4, 3], 2, False),
+]
+
+
+@pytest.fixture(scope='module')
+def nd_cache(bb, torch_cuda):
+    """One JIT cache for the nd callback tests: they need four distinct kernels per precision
+    (c2c with load, c2c with store, r2c with load, c2r with store)."""
+    return bb.Cache()
+
+
+@pytest.mark.parametrize('which', ['both', 'load', 'store'])
+@pytest.mark.parametrize('prec', [4, 8])
+@pytest.mark.parametrize('case', ND_CASES, ids=['x'.join(map(str, c[1])) + ['-c2c', '-r2c', '-c2r'][c[2]]
+                                                + ('-inplace' if c[3] else '') for c in ND_CASES])
+def test_nd_callbacks(bb, po, torch_cuda, nd_cache, case, prec, which):
+    """nd plans with callbacks (the reference rejects them, src/common/algorithm/nd_fft.hpp:29-31):
+    the load function weights every input element by its input-tensor offset, the store
+    function every output element by its output-tensor offset; against the FP64 DFT of the
+    weighted input, weighted at the output."""
+    torch = torch_cuda
+    dim, shape, type, inplace = case
+    T, T2 = _types(prec)
+    src = ND_SRC.format(T=T, T2=T2)
+    load = 'load_w' if which in ('both', 'load') else None
+    store = 'store_w' if which in ('both', 'store') else None
+    d = bb.BACKWARD if type == 2 else bb.FORWARD
+    cfg = bb.configuration(dim, shape, precision=prec, type=type, direction=d, inplace=inplace,
+                           callbacks=(src, load, store))
+    ist, ost = list(cfg.istride), list(cfg.ostride)
+    n1in = shape[1] // 2 + 1 if type == 2 else shape[1]
+    n1out = shape[1] // 2 + 1 if type == 1 else shape[1]
+    ishape = [shape[0], n1in] + shape[2:dim + 2]
+    oshape = [shape[0], n1out] + shape[2:dim + 2]
+    isize = po.tensor_size(dim, ishape, ist)
+    osize = po.tensor_size(dim, oshape, ost)
+    rdt, cdt = dtypes(prec)
+    rng = np.random.default_rng(sum(shape) * 7 + type + prec)
+    if type == 1:
+        x = rng.standard_normal(isize).astype(rdt)
+    else:
+        x = (rng.standard_normal(isize) + 1j * rng.standard_normal(isize)).astype(cdt)
+    plan = bb.Plan(cfg, stream=torch.cuda.current_stream().cuda_stream, cache=nd_cache)
+    out = run(bb, torch, cfg, x, osize, rdt if type == 2 else cdt, inplace=inplace, plan=plan)
+    xw = x.astype(np.float64 if type == 1 else np.complex128)
+    if load:
+        xw = xw * (1.0 + (np.arange(isize) % 5) * 0.25)
+    ref = po.dft64(dim, shape, type, d, po.gather(xw, dim, ishape, ist))
+    if store:
+        ref = ref * (1.0 + (po.gather(np.arange(osize), dim, oshape, ost) % 3) * 0.5)
+    got = po.gather(out, dim, oshape, ost)
+    assert rel_l2(got, ref) <= TOL[prec]
+    info = plan.info()
+    assert info.num_launches == dim and info.jit_compiled == 1
