@@ -24,6 +24,7 @@ on the host cores with the same metric.
 """
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -39,6 +40,9 @@ for _p in (REPO, PKG):
         sys.path.insert(0, _p)
 
 SWEEP_N = [16, 32, 64, 128, 256, 512, 48, 96, 160, 224, 384, 7, 11, 13]
+# secondary legs, in the order they run (the peaks first: later legs use them)
+LEGS = ['peaks', 'c2c_n64_k16384', 'ragged_10k', 'spectral_layer_2d', 'c2c_3d_64',
+        'tft_vs_double_batched', 'sweep_f64', 'tensor_core_c2c', 'cufft', 'sweep_all_n']
 M_BATCH = 8
 REAL_BYTES = 1 << 30
 METRIC = 'GB/s vs HBM peak per N; plain vs split-TC form at rel-L2<=1e-6 vs FP64'
@@ -50,6 +54,12 @@ def k_for(N, prec):
 
 def pass_bytes(N, K, prec, M=M_BATCH):
     return (N * prec + (N // 2 + 1) * 2 * prec) * M * K
+
+
+def pass_flops(N, K, M=M_BATCH, real=True):
+    """The reference's flop model (benchmark/adapter.hpp:21-25,51-52): 5 N log2 N per
+    complex transform, 2.5 N log2 N per real one."""
+    return (2.5 if real else 5.0) * N * math.log2(N) * M * K
 
 
 def measured_peaks():
@@ -276,6 +286,8 @@ def run_ours(args):
         dist.barrier()
     ms_per_step = t_ms / args.steps
     value = total_bytes * ws / (ms_per_step * 1e-3) / 1e9
+    total_flops = sum(2 * pass_flops(N, K) for (N, K, _, _) in plans)
+    gflops = total_flops * ws / (ms_per_step * 1e-3) / 1e9
 
     # per-launch durations (events around each launch inside the timed region)
     per_n = []
@@ -285,8 +297,10 @@ def run_ours(args):
         tb = np.mean([ev[s][4 * i + 2].elapsed_time(ev[s][4 * i + 3]) for s in range(args.steps)])
         kernel_ms += tf + tb
         pbytes = pass_bytes(N, K, prec)
+        pfl = pass_flops(N, K)
         per_n.append({'N': N, 'K': K, 'r2c_gbs': round(pbytes / tf / 1e6, 1),
                       'c2r_gbs': round(pbytes / tb / 1e6, 1),
+                      'r2c_gflops': round(pfl / tf / 1e6, 1), 'c2r_gflops': round(pfl / tb / 1e6, 1),
                       'r2c_frac': round(pbytes / tf / 1e6 / hbm_peak, 3),
                       'c2r_frac': round(pbytes / tb / 1e6 / hbm_peak, 3)})
     achieved = total_bytes / (kernel_ms * 1e-3) / 1e9
@@ -301,16 +315,33 @@ def run_ours(args):
     del xbuf, Xbuf, ybuf
     torch.cuda.empty_cache()
     legs = {}
+    wanted = LEGS if args.legs == 'all' else [w for w in args.legs.split(',') if w]
     if not args.no_legs and rank == 0:
-        legs['c2c_n64_k16384'] = leg_c2c_cfg1(bb, torch, stream, hbm_peak, args.steps, args.warmup)
-        legs['ragged_10k'] = leg_ragged(bb, torch, stream, hbm_peak, args.steps, args.warmup)
-        legs['spectral_layer_2d'] = leg_spectral(bb, torch, stream, args.steps, args.warmup)
-        legs['c2c_3d_64'] = leg_c2c_3d(bb, torch, stream, hbm_peak, args.steps, args.warmup)
-        legs['tft_vs_double_batched'] = leg_tft(bb, torch, stream, hbm_peak, args.steps, args.warmup)
-        legs['sweep_f64'] = leg_sweep_f64(bb, torch, stream, hbm_peak, max(2, args.steps // 2), 1)
-        torch.cuda.empty_cache()
-        legs['tensor_core_c2c'] = leg_tensor_core(bb, torch, stream, hbm_peak, args.steps, args.warmup)
-        torch.cuda.empty_cache()
+        peaks = None
+        runners = {
+            'peaks': lambda: leg_peaks(torch, stream),
+            'c2c_n64_k16384': lambda: leg_c2c_cfg1(bb, torch, stream, hbm_peak, args.steps, args.warmup),
+            'ragged_10k': lambda: leg_ragged(bb, torch, stream, hbm_peak, args.steps, args.warmup),
+            'spectral_layer_2d': lambda: leg_spectral(bb, torch, stream, args.steps, args.warmup),
+            'c2c_3d_64': lambda: leg_c2c_3d(bb, torch, stream, hbm_peak, args.steps, args.warmup),
+            'tft_vs_double_batched': lambda: leg_tft(bb, torch, stream, hbm_peak, args.steps, args.warmup),
+            'sweep_f64': lambda: leg_sweep_f64(bb, torch, stream, hbm_peak, max(2, args.steps // 2), 1,
+                                               peaks),
+            'tensor_core_c2c': lambda: leg_tensor_core(bb, torch, stream, hbm_peak, args.steps,
+                                                       args.warmup, peaks),
+            'cufft': lambda: leg_cufft(bb, torch, stream, hbm_peak, plans),
+            'sweep_all_n': lambda: leg_sweep_all_n(bb, torch, stream, hbm_peak),
+        }
+        for name in wanted:
+            if name not in runners:
+                raise SystemExit('unknown leg ' + name)
+            try:
+                legs[name] = runners[name]()
+            except (RuntimeError, OSError) as e:  # one failing leg does not lose the line
+                legs[name] = {'error': str(e)[:300]}
+            if name == 'peaks' and 'error' not in legs[name]:
+                peaks = legs[name]
+            torch.cuda.empty_cache()
 
     line = {
         'metric': METRIC, 'value': round(value, 1), 'unit': 'GB/s', 'n_gpus': ws,
@@ -325,6 +356,8 @@ def run_ours(args):
                      'algorithmic_bytes': total_bytes, 'per': 'step (28 launches)',
                      'peak_kind': peak_kind, 'kernel': 'fft_kernel_ct<float, kind, ...> (all '
                      'launches of the step; algorithmic bytes = one read + one write)'},
+        'gflops': {'value': round(gflops, 1), 'unit': 'GFLOP/s',
+                   'model': '2.5 N log2 N per real transform (reference benchmark/adapter.hpp:51-52)'},
         'per_n': per_n,
         'clocks': clk,
         'e2e': e2e,
@@ -351,9 +384,12 @@ def event_time(torch, stream, fn, reps):
     return e0.elapsed_time(e1) / reps
 
 
-def leg_sweep_f64(bb, torch, stream, hbm_peak, steps, warmup):
-    """Same r2c+c2r sweep in float64 (FP64 arithmetic is the bound on GB300)."""
+def leg_sweep_f64(bb, torch, stream, hbm_peak, steps, warmup, peaks=None):
+    """Same r2c+c2r sweep in float64.  Each launch is also reported against its roofline
+    min(HBM, FP64 peak / flop-per-byte) with the reference's flop model (2.5 N log2 N per
+    real transform) and the FP64 FMA peak measured by the peaks leg."""
     sptr = stream.cuda_stream
+    fp64 = peaks['fp64_tflops'] if peaks else None
     out = []
     tot_b, tot_ms = 0, 0.0
     x = torch.randn((1 << 30) // 8, dtype=torch.float64, device='cuda')
@@ -371,13 +407,189 @@ def leg_sweep_f64(bb, torch, stream, hbm_peak, steps, warmup):
         tf = event_time(torch, stream, lambda: f.execute(x.data_ptr(), X.data_ptr()), steps)
         tb = event_time(torch, stream, lambda: b.execute(X.data_ptr(), y.data_ptr()), steps)
         pb = pass_bytes(N, K, 8)
+        pf = pass_flops(N, K)
         tot_b += 2 * pb
         tot_ms += tf + tb
-        out.append({'N': N, 'r2c_gbs': round(pb / tf / 1e6, 1), 'c2r_gbs': round(pb / tb / 1e6, 1)})
-    return {'value': round(tot_b / tot_ms / 1e6, 1), 'unit': 'GB/s',
-            'frac_of_hbm': round(tot_b / tot_ms / 1e6 / hbm_peak, 3),
-            'note': 'r2c+c2r M=8, 1 GiB real input per N, float64; FP64-compute-bound on GB300',
-            'per_n': out}
+        rec = {'N': N, 'r2c_gbs': round(pb / tf / 1e6, 1), 'c2r_gbs': round(pb / tb / 1e6, 1),
+               'r2c_gflops': round(pf / tf / 1e6, 1), 'c2r_gflops': round(pf / tb / 1e6, 1)}
+        if fp64:
+            # attainable GB/s of this launch: min(HBM, FP64 peak / (flops per byte))
+            bound = min(hbm_peak, fp64 * 1e3 * pb / pf)
+            rec['roofline_gbs'] = round(bound, 1)
+            rec['r2c_frac'] = round(pb / tf / 1e6 / bound, 3)
+            rec['c2r_frac'] = round(pb / tb / 1e6 / bound, 3)
+        out.append(rec)
+    res = {'value': round(tot_b / tot_ms / 1e6, 1), 'unit': 'GB/s',
+           'frac_of_hbm': round(tot_b / tot_ms / 1e6 / hbm_peak, 3),
+           'note': 'r2c+c2r M=8, 1 GiB real input per N, float64',
+           'per_n': out}
+    if fp64:
+        tot_bound_ms = sum(2 * pass_bytes(r['N'], k_for(r['N'], 8), 8) / r['roofline_gbs'] / 1e6
+                           for r in out)
+        res['fp64_peak_tflops'] = fp64
+        res['frac_of_roofline'] = round(tot_bound_ms / tot_ms, 3)
+        res['roofline'] = ('per launch min(HBM, FP64 FMA peak x bytes / model flops), model flops '
+                           '2.5 N log2 N per real transform')
+    return res
+
+
+def probes_lib():
+    import ctypes
+
+    lib = ctypes.CDLL(os.path.join(PKG, 'bbfft_gb300', '_lib', 'libbbfft_probes.so'))
+    for f in ('gbfft_probe_dfma', 'gbfft_probe_ffma', 'gbfft_probe_mma_tf32', 'gbfft_probe_mma_bf16'):
+        getattr(lib, f).argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                    ctypes.c_void_p]
+    return lib
+
+
+def leg_peaks(torch, stream, seconds=0.6):
+    """Measured throughput of the pipes the transforms can be bound by, besides HBM: the
+    FP64 and FP32 FMA pipes (independent FMA chains in registers) and the warp-level MMAs
+    of the tensor-core stages (mma.sync TF32 m16n8k8, BF16 m16n8k16), each timed with CUDA
+    events over about `seconds` of back-to-back work, SM clock sampled meanwhile."""
+    lib = probes_lib()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, threads = sms * 8, 256
+    out = torch.empty(blocks * threads, dtype=torch.float64, device='cuda')
+    sptr = stream.cuda_stream
+    chains, acc = 8, 4
+    kinds = {
+        # name: (entry, flops per iteration per thread)
+        'fp64_tflops': (lib.gbfft_probe_dfma, 2 * chains),
+        'fp32_tflops': (lib.gbfft_probe_ffma, 2 * chains),
+        'mma_tf32_tflops': (lib.gbfft_probe_mma_tf32, 2 * 16 * 8 * 8 * acc / 32),
+        'mma_bf16_tflops': (lib.gbfft_probe_mma_bf16, 2 * 16 * 8 * 16 * acc / 32),
+    }
+    res = {}
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    for name, (fn, fpi) in kinds.items():
+        iters = 256
+        for _ in range(12):  # calibrate: grow until one launch takes >= 20 ms
+            ms = event_time(torch, stream, lambda: fn(blocks, threads, iters, out.data_ptr(), sptr), 1)
+            if ms >= 20.0 or iters >= (1 << 24):
+                break
+            iters = int(iters * min(16.0, max(2.0, 25.0 / max(ms, 1e-3))))
+        reps = max(1, int(seconds * 1e3 / ms))
+        ms = event_time(torch, stream, lambda: fn(blocks, threads, iters, out.data_ptr(), sptr), reps)
+        res[name] = round(blocks * threads * iters * fpi / (ms * 1e-3) / 1e12, 2)
+    clk = clocks.stop()
+    res['clocks'] = clk
+    res['how'] = ('%d CTAs x %d threads; FMA: %d independent chains per thread; MMA: %d '
+                  'independent accumulator tiles per warp; CUDA events' % (blocks, threads, chains, acc))
+    return res
+
+
+def leg_cufft(bb, torch, stream, hbm_peak, plans):
+    """cuFFT on the headline shapes beside this library's launches: r2c + c2r, M = 8,
+    1 GiB real input per N, float32, through torch.fft over the N mode of the (K, N, M)
+    tensor (cuFFT rejects the reference's per-m loop, benchmark/test-cufft.cpp:38-45, for
+    real data: a real tensor offset by one float is not a valid cuFFT pointer); and c2c
+    M = 8 the reference's way, one cufftPlanMany over K executed once per m."""
+    from bbfft_gb300 import cufft
+
+    sptr = stream.cuda_stream
+    maxr = max(M_BATCH * N * k_for(N, 4) for N in SWEEP_N)
+    maxc = max(M_BATCH * (N // 2 + 1) * k_for(N, 4) for N in SWEEP_N)
+    x = torch.randn(maxr, device='cuda')
+    X = torch.empty(2 * maxc, device='cuda')
+    y = torch.empty(maxr, device='cuda')
+    rows, tot_b, tot_ours, tot_cu = [], 0, 0.0, 0.0
+    for (N, K, pf, pb) in plans:
+        xv = x[:M_BATCH * N * K].view(K, N, M_BATCH)
+        Xv = torch.view_as_complex(X[:2 * M_BATCH * (N // 2 + 1) * K].view(K, N // 2 + 1, M_BATCH, 2))
+        yv = y[:M_BATCH * N * K].view(K, N, M_BATCH)
+
+        def tfft():
+            torch.fft.rfft(xv, dim=1, out=Xv)
+            torch.fft.irfft(Xv, n=N, dim=1, norm='forward', out=yv)
+
+        tfft()
+        t_cu = event_time(torch, stream, tfft, 3)
+        t_ours = event_time(torch, stream, lambda: (pf.execute(x.data_ptr(), X.data_ptr()),
+                                                    pb.execute(X.data_ptr(), y.data_ptr())), 3)
+        b = 2 * pass_bytes(N, K, 4)
+        tot_b += b
+        tot_ours += t_ours
+        tot_cu += t_cu
+        # c2c, M = 8, the reference's cuFFT loop over m (complex offsets are valid pointers)
+        Kc = (1 << 30) // (8 * M_BATCH * N)
+        cp = cufft.Plan(4, 'c2c', M_BATCH, N, Kc, sptr)
+        op = bb.Plan(bb.configuration(1, [M_BATCH, N, Kc], precision=bb.F32), stream=sptr)
+        cp.execute(x.data_ptr(), y.data_ptr())
+        op.execute(x.data_ptr(), y.data_ptr())
+        t_cc = event_time(torch, stream, lambda: cp.execute(x.data_ptr(), y.data_ptr()), 3)
+        t_oc = event_time(torch, stream, lambda: op.execute(x.data_ptr(), y.data_ptr()), 3)
+        cp.destroy()
+        bc = 2 * M_BATCH * N * Kc * 8
+        rows.append({'N': N, 'r2c_c2r_torch_fft_gbs': round(b / t_cu / 1e6, 1),
+                     'r2c_c2r_ours_gbs': round(b / t_ours / 1e6, 1),
+                     'c2c_cufft_loop_gbs': round(bc / t_cc / 1e6, 1),
+                     'c2c_ours_gbs': round(bc / t_oc / 1e6, 1)})
+    return {'r2c_c2r_torch_fft_gbs': round(tot_b / tot_cu / 1e6, 1),
+            'r2c_c2r_ours_gbs': round(tot_b / tot_ours / 1e6, 1),
+            'speedup_vs_torch_fft': round(tot_cu / tot_ours, 2), 'per_n': rows,
+            'how': 'r2c+c2r: torch.fft.rfft / irfft over dim 1 of the (K, N, 8) tensor (cuFFT), '
+                   '1 GiB real input per N; c2c: cufftPlanMany over K (stride 8, distance 8N) '
+                   'executed once per m, 1 GiB complex input per N; float32, CUDA events'}
+
+
+ALL_N = list(range(16, 513))
+
+
+def leg_sweep_all_n(bb, torch, stream, hbm_peak, reps=2):
+    """Every N in 16..512, float32, each launch on a 1 GiB input: c2c forward at M = 1 and
+    M = 8, r2c and c2r at M = 8; GB/s (one read + one write) as fractions of the measured
+    HBM bandwidth, and cuFFT's c2c M = 1 beside them."""
+    from bbfft_gb300 import cufft
+
+    sptr = stream.cuda_stream
+    cap = (1 << 28) + (1 << 25)  # floats: 1.125 GiB covers every input and output
+    x = torch.randn(cap, device='cuda')
+    y = torch.empty(cap, device='cuda')
+    z = torch.empty(cap, device='cuda')
+    res = {k: [] for k in ('c2c_m1', 'c2c_m8', 'r2c_m8', 'c2r_m8', 'cufft_c2c_m1')}
+    t0 = time.perf_counter()
+    for N in ALL_N:
+        cases = [
+            ('c2c_m1', bb.configuration(1, [1, N, (1 << 30) // (8 * N)], precision=bb.F32), x, y,
+             2 * N * 8 * ((1 << 30) // (8 * N))),
+            ('c2c_m8', bb.configuration(1, [8, N, (1 << 30) // (64 * N)], precision=bb.F32), x, y,
+             2 * 8 * N * 8 * ((1 << 30) // (64 * N))),
+        ]
+        K = (1 << 30) // (32 * N)
+        cases.append(('r2c_m8', bb.configuration(1, [8, N, K], precision=bb.F32, type=bb.R2C), x, y,
+                      pass_bytes(N, K, 4)))
+        cases.append(('c2r_m8', bb.configuration(1, [8, N, K], precision=bb.F32, type=bb.C2R,
+                                                 direction=bb.BACKWARD), y, z, pass_bytes(N, K, 4)))
+        for name, cfg, a, b, nbytes in cases:
+            plan = bb.Plan(cfg, stream=sptr)
+            plan.execute(a.data_ptr(), b.data_ptr())
+            ms = event_time(torch, stream, lambda: plan.execute(a.data_ptr(), b.data_ptr()), reps)
+            res[name].append(round(nbytes / ms / 1e6 / hbm_peak, 3))
+            del plan
+        Kc = (1 << 30) // (8 * N)
+        cp = cufft.Plan(4, 'c2c', 1, N, Kc, sptr)
+        cp.execute(x.data_ptr(), y.data_ptr())
+        ms = event_time(torch, stream, lambda: cp.execute(x.data_ptr(), y.data_ptr()), reps)
+        res['cufft_c2c_m1'].append(round(2 * N * 8 * Kc / ms / 1e6 / hbm_peak, 3))
+        cp.destroy()
+    summary = {}
+    for k, v in res.items():
+        arr = np.array(v)
+        worst = np.argsort(arr)[:8]
+        summary[k] = {'at_least_0.8': int((arr >= 0.8).sum()), 'of': len(v),
+                      'min': float(arr.min()), 'median': float(np.median(arr)),
+                      'worst': [[ALL_N[i], float(arr[i])] for i in worst]}
+    mult8 = [i for i, N in enumerate(ALL_N) if N % 8 == 0]
+    for k in ('c2c_m1', 'c2c_m8', 'r2c_m8', 'c2r_m8'):
+        summary[k]['multiples_of_8_at_least_0.8'] = int(sum(res[k][i] >= 0.8 for i in mult8))
+        summary[k]['multiples_of_8'] = len(mult8)
+    return {'unit': 'fraction of measured HBM bandwidth', 'N': [ALL_N[0], ALL_N[-1]],
+            'summary': summary, 'frac': res, 'seconds': round(time.perf_counter() - t0, 1),
+            'how': 'plan per (N, kind), 1 warm-up launch, %d timed (CUDA events); inputs 1 GiB '
+                   '(> L2)' % reps}
 
 
 def leg_c2c_cfg1(bb, torch, stream, hbm_peak, steps, warmup):
@@ -544,15 +756,24 @@ def leg_c2c_3d(bb, torch, stream, hbm_peak, steps, warmup):
             'frac_of_hbm': round(bytes_ / ms / 1e6 / hbm_peak, 3)}
 
 
-def leg_tensor_core(bb, torch, stream, hbm_peak, steps, warmup):
+# MMAs (mma.sync m16n8k8 TF32, 2048 flops each with the padding) per transform of the
+# split-TF32 form: a radix-P stage on the tensor cores runs 2 (cosine, sine) x KS^2 x 3
+# (split products) MMAs per 8 butterflies, KS = ceil((P/2 - 1) / 8): 3 per radix-32
+# butterfly, 0.75 per radix-16 one.  64 = 32 x 2, 256 = 16 x 16, 512 = 32 x 16.
+TF32_MMAS_PER_TRANSFORM = {64: 2 * 3, 256: 32 * 0.75, 512: 16 * 3 + 32 * 0.75}
+
+
+def leg_tensor_core(bb, torch, stream, hbm_peak, steps, warmup, peaks=None):
     """c2c forward, M=1, K=2^20, N in {64, 256, 512}, N(0,1) inputs with a 1e-3 fraction
     scaled by 1e4: plain FP32 against the tensor-core forms, GB/s and rel-L2 against FP64
-    on a 4096-transform slice."""
+    on a 4096-transform slice; for the split-TF32 form also its MMA throughput against the
+    measured mma.sync TF32 peak."""
     from oracle import pyoracle as po
 
     sptr = stream.cuda_stream
     K = 1 << 20
     out = {}
+    tf32_peak = peaks.get('mma_tf32_tflops') if peaks else None
     for N in (64, 256, 512):
         g = torch.Generator(device='cuda')
         g.manual_seed(N)
@@ -563,7 +784,8 @@ def leg_tensor_core(bb, torch, stream, hbm_peak, steps, warmup):
         xs = x[:2 * N * 4096].cpu().numpy().view(np.complex64).astype(np.complex128)
         ref = po.dft64(1, [1, N, 4096], po.C2C, po.FORWARD, xs.reshape(4096, N, 1))
         row = {}
-        for name, mode in (('fp32', 0), ('bf16', 1), ('split_bf16_3term', 3), ('split_bf16_6term', 2)):
+        for name, mode in (('fp32', 0), ('bf16', 1), ('split_bf16_3term', 3), ('split_bf16_6term', 2),
+                           ('split_tf32_3term', 4)):
             plan = bb.Plan(bb.configuration(1, [1, N, K], precision=bb.F32, compute=mode), stream=sptr)
             for _ in range(warmup):
                 plan.execute(x.data_ptr(), y.data_ptr())
@@ -573,6 +795,11 @@ def leg_tensor_core(bb, torch, stream, hbm_peak, steps, warmup):
             gbs = 2 * N * K * 8 / ms / 1e6
             row[name] = {'gbs': round(gbs, 1), 'frac_of_hbm': round(gbs / hbm_peak, 3),
                          'rel_l2': float('%.3g' % err)}
+            if mode == 4:
+                tfl = TF32_MMAS_PER_TRANSFORM[N] * 2048 * K / ms / 1e9
+                row[name]['mma_tflops'] = round(tfl, 1)
+                if tf32_peak:
+                    row[name]['frac_of_mma_tf32_peak'] = round(tfl / tf32_peak, 3)
         out['N%d' % N] = row
         del x, y
     return out
@@ -725,6 +952,8 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--cpu-seconds', type=float, default=15.0)
     ap.add_argument('--no-legs', action='store_true', help='headline workload only')
+    ap.add_argument('--legs', default='all',
+                    help='comma-separated secondary legs to run (default: all): ' + ','.join(LEGS))
     ap.add_argument('--profile', choices=['step', 'case', 'ragged'], help='launches for an ncu capture')
     ap.add_argument('--profile-case', default='c2r:160')
     args = ap.parse_args()

@@ -19,6 +19,9 @@ INCLUDE = os.path.join(REPO, 'include')
 OUTDIR = os.path.join(HERE, 'bbfft_gb300', '_lib')
 BUILD = os.path.join(HERE, '_build')
 LIB = os.path.join(OUTDIR, 'libbbfft_gb300.so')
+# throughput probes for the benchmark's roofline denominators (not part of the library)
+PROBES_SRC = os.path.join(CSRC, 'peak_probes.cu')
+PROBES_LIB = os.path.join(OUTDIR, 'libbbfft_probes.so')
 
 ARCH = '-gencode=arch=compute_103a,code=sm_103a'
 ENGINE_HEADERS = ['params.h', 'root_of_unity_table.cuh', 'radix.cuh', 'engine.cuh']
@@ -119,6 +122,10 @@ def build(verbose=False, jobs=None):
         if newer(obj, [src] + headers + [os.path.join(BUILD, 'engine_src.inc')]):
             jobs_list.append([cxx, '-O2', '-std=c++17', '-fPIC', '-fvisibility=hidden', '-Wall',
                               '-c', src, '-o', obj] + common_inc)
+    if newer(PROBES_LIB, [PROBES_SRC]):
+        jobs_list.append([nvcc, ARCH, '-lineinfo', '-O3', '-std=c++17', '-shared', '-Xcompiler',
+                          '-fPIC', PROBES_SRC, '-o', PROBES_LIB, '-L' + os.path.join(cuda, 'lib64'),
+                          '-lcudart'])
     if jobs_list:
         with cf.ThreadPoolExecutor(max_workers=jobs or max(1, os.cpu_count() or 1)) as ex:
             outs = list(ex.map(run, jobs_list))

@@ -775,6 +775,9 @@ std::string callback_program(const char *cb, std::size_t len, const char *load_f
                              std::vector<std::tuple<std::string, int, int, int>> const &kernels) {
     std::ostringstream src;
     src << "typedef decltype(sizeof(0)) size_t;\n";
+    // NVRTC kernels keep the CUDA-core odd-radix stages (the tensor-core stages'
+    // coefficient tables are not part of the embedded engine source)
+    src << "#define GBFFT_NVRTC 1\n";
     src << kEngineSource << "\n";
     src << std::string(cb, len) << "\n";
     std::set<int> ios;
@@ -1218,6 +1221,15 @@ const char *plan_pass_fixed(int prec, int type, int dir, long long M, long long 
         rad[L++] = r0[i];
     }
     bool post = kind == kind_r2c_half;
+    // a generic odd-radix stage reads and writes shared memory only (its tensor-core form
+    // writes the butterflies of several transforms per warp): a copy stage follows it, as
+    // in make_1d_pass
+    if (!post && table_generic(rad[L - 1])) {
+        if (L >= max_stages) {
+            return "too many stages";
+        }
+        rad[L++] = 1;
+    }
     if (is_real && !post && L == 1) {
         rad[L++] = 1;
     }
@@ -1315,7 +1327,7 @@ const char *plan_pass_fixed(int prec, int type, int dir, long long M, long long 
     grid = static_cast<unsigned>(p.m_tiles * k_tiles);
     block = static_cast<unsigned>(Mb * T * Kb);
     func = ct ? ct->fn : (prec == 4 ? kernel_f32(kind) : kernel_f64(kind));
-    if (smem > 48 * 1024 &&
+    if (needs_smem_optin(smem) &&
         cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
         return "cudaFuncSetAttribute failed";
     }
@@ -1588,8 +1600,18 @@ static void execute_impl(bbfft_plan_s &plan, const void *in, void *out, cudaStre
     }
     int cur = -1;
     GB_CUDA(cudaGetDevice(&cur));
+    // the caller's device is current again on every way out, errors included
+    struct restore_device {
+        int cur, dev;
+        ~restore_device() {
+            if (cur != dev) {
+                cudaSetDevice(cur);
+            }
+        }
+    } restore{cur, cur};
     if (cur != plan.device) {
         GB_CUDA(cudaSetDevice(plan.device));
+        restore.dev = plan.device;
     }
     void *packed_in = plan.packed_in ? plan.packed_in->ptr : nullptr;
     void *packed_out = plan.packed_out ? plan.packed_out->ptr : nullptr;
@@ -1618,9 +1640,6 @@ static void execute_impl(bbfft_plan_s &plan, const void *in, void *out, cudaStre
             void *cargs[] = {&cp};
             cudaError_t e = cudaLaunchKernel(pass0.func, dim3(pass0.grid), dim3(pass0.block), cargs, 0, stream);
             if (e != cudaSuccess) {
-                if (cur != plan.device) {
-                    cudaSetDevice(cur);
-                }
                 throw status_error(BBFFT_CUDA_ERROR,
                                    std::string("kernel launch failed: ") + cudaGetErrorString(e));
             }
@@ -1647,15 +1666,9 @@ static void execute_impl(bbfft_plan_s &plan, const void *in, void *out, cudaStre
         void *args[] = {&p};
         cudaError_t e = cudaLaunchKernel(ps.func, dim3(ps.grid), dim3(ps.block), args, ps.smem, stream);
         if (e != cudaSuccess) {
-            if (cur != plan.device) {
-                cudaSetDevice(cur);
-            }
             throw status_error(BBFFT_CUDA_ERROR,
                                std::string("kernel launch failed: ") + cudaGetErrorString(e));
         }
-    }
-    if (cur != plan.device) {
-        GB_CUDA(cudaSetDevice(cur));
     }
 }
 
@@ -2070,7 +2083,9 @@ int bbfft_aot_generate(const bbfft_configuration *cfgs, size_t num_cfgs, void *i
                 add(kind, c.load_function, c.store_function);
             } else {
                 // the passes of an nd plan that call user functions: the first (load) and
-                // the last (store); c2r runs the outer modes first and its real pass last
+                // the last (store); c2r runs the outer modes first and its real pass last.
+                // An nd plan always has dim >= 2 passes (make_plan_impl keeps modes of
+                // size 1), so no pass calls both functions.
                 bool c2r = c.type == BBFFT_C2R;
                 add(c2r ? gbfft::kind_c2c : kind, c.load_function, nullptr);
                 add(c2r ? kind : gbfft::kind_c2c, nullptr, c.store_function);

@@ -1,8 +1,10 @@
 // Allocation-free 2d c2r transform.
 //
-// Some callers cannot allocate device memory at the point where they need a transform:
-// code running while a CUDA graph is being captured, allocators that forbid cudaMalloc
-// after start-up, or hosts that must not grow their device footprint.  The regular nd c2r
+// Some callers cannot allocate device memory at the point where they need a transform: a
+// process whose memory manager reserves the device memory at start-up and forbids
+// cudaMalloc afterwards (cudaMalloc would then fail, or silently take memory the manager
+// has promised elsewhere), or a host that must not grow its device footprint after
+// start-up.  The regular nd c2r
 // plan allocates a temporary buffer (the reference's nd_fft does the same,
 // src/common/algorithm/nd_fft.hpp:114-125) and twiddle tables at plan creation.  The entry
 // point below instead keeps its temporary and its twiddles in file-scope device arrays
@@ -83,6 +85,9 @@ extern "C" int bbfft_c2r_2d_noalloc_f32(const void *in, void *out, size_t M, siz
                                         size_t K, cudaStream_t stream) {
     using namespace gbfft;
     clear_fixed_error();
+    // an error left on this thread by earlier, unrelated work must not be reported as a
+    // failure of this call
+    (void)cudaGetLastError();
     if (!in || !out) {
         set_fixed_error("null tensor pointer");
         return BBFFT_INVALID_ARGUMENT;
@@ -143,8 +148,13 @@ extern "C" int bbfft_c2r_2d_noalloc_f32(const void *in, void *out, size_t M, siz
     }
     float2 *tw0 = st->twiddles;
     float2 *tw1 = st->twiddles + kNoAllocMaxN;
-    noalloc_twiddle_kernel<<<(p[0].Nt + 127) / 128, 128, 0, stream>>>(tw0, p[0].Nt);
-    noalloc_twiddle_kernel<<<(p[1].Nt + 127) / 128, 128, 0, stream>>>(tw1, p[1].Nt);
+    for (int i = 0; i < 2; ++i) {
+        noalloc_twiddle_kernel<<<(p[i].Nt + 127) / 128, 128, 0, stream>>>(i ? tw1 : tw0, p[i].Nt);
+        if (cudaGetLastError() != cudaSuccess) {
+            set_fixed_error("twiddle kernel launch failed in the allocation-free c2r");
+            return BBFFT_CUDA_ERROR;
+        }
+    }
     p[0].in = in;
     p[0].out = st->scratch;
     p[0].tw = tw0;
@@ -159,10 +169,6 @@ extern "C" int bbfft_c2r_2d_noalloc_f32(const void *in, void *out, size_t M, siz
             set_fixed_error("kernel launch failed in the allocation-free c2r");
             return BBFFT_CUDA_ERROR;
         }
-    }
-    if (cudaGetLastError() != cudaSuccess) {
-        set_fixed_error("kernel launch failed in the allocation-free c2r");
-        return BBFFT_CUDA_ERROR;
     }
     return BBFFT_SUCCESS;
 }

@@ -262,17 +262,21 @@ BBFFT_GB300_API int bbfft_ragged_get_info(bbfft_ragged_t ragged, bbfft_ragged_in
 BBFFT_GB300_API int bbfft_ragged_destroy(bbfft_ragged_t ragged);
 
 /* Allocation-free 2d c2r, float precision.  No counterpart in the reference: it exists for
- * callers that cannot allocate device memory when they transform (during CUDA graph
- * capture, under allocators that forbid cudaMalloc, or with a fixed device footprint).
- * Same result as a plan of {dim 2, shape {M, N1, N2, K}, f32, backward, c2r} with the
- * default out-of-place layout, but the temporary between the two passes and the
- * twiddle tables live in static device arrays of the library (16 MiB + 8 KiB held on
- * every GPU that loads the library until the process exits).  Limits: N1, N2 <= 512 and
+ * callers that cannot allocate device memory when they transform -- a process whose
+ * memory manager reserves the device memory at start-up and forbids cudaMalloc later, or
+ * a host that must keep a fixed device footprint -- while a plan allocates its
+ * temporary and twiddle tables.  The result equals that of a plan of {dim 2, shape
+ * {M, N1, N2, K}, f32, backward, c2r} with the default out-of-place layout within float
+ * rounding (rel-L2 <= 2e-6), but the temporary between the two passes and the twiddle
+ * tables live in static device arrays of the library (16 MiB + 8 KiB held on every GPU
+ * that loads the library until the process exits).  Limits: N1, N2 <= 512 and
  * M * (N1/2+1) * N2 * K <= 2^21; larger problems return BBFFT_BAD_CONFIGURATION.  It
  * calls no cudaMalloc, cudaFree or other allocating routine.  The first call on a device
- * resolves the device addresses of the static arrays.  All calls share the arrays, so
- * calls that may overlap on the GPU (different streams, different host threads) race;
- * serialise them.  Out-of-place only (in != out). */
+ * resolves the device addresses of the static arrays (cudaGetSymbolAddress) with that
+ * device current; make that first call before any stream capture begins.  All calls
+ * share the arrays and every call rewrites what it uses, so calls that may overlap on
+ * the GPU (different streams, different host threads) race; serialise them.
+ * Out-of-place only (in != out). */
 BBFFT_GB300_API int bbfft_c2r_2d_noalloc_f32(const void *in, void *out, size_t M, size_t N1,
                                              size_t N2, size_t K, cudaStream_t stream);
 

@@ -1,12 +1,15 @@
 """The allocation-free 2d c2r entry point (bbfft_c2r_2d_noalloc_f32) against a regular plan.
 
-Callers that cannot allocate device memory when they transform -- code running while a
-CUDA graph is captured, allocators that forbid cudaMalloc after start-up -- use this entry
-point: its temporary and twiddles live in static device arrays of the library instead of
-buffers that a plan allocates.  The test calls it through the C ABI twice in a row (the
-second call reuses the shared static arrays with another shape and other data) and
-requires the result of the regular nd c2r plan within the float tolerance of the parity
-tests (rel-L2 <= 2e-6).
+Callers that cannot allocate device memory when they transform -- a process whose memory
+manager reserves the device at start-up and forbids cudaMalloc later, or a host that must
+keep a fixed device footprint -- use this entry point: its temporary and twiddles live in
+static device arrays of the library instead of buffers that a plan allocates.  The test
+calls it through the C ABI several times in a row (each call reuses the shared static
+arrays with another shape and other data) and requires the result of the regular nd c2r
+plan within the float tolerance of the parity tests (rel-L2 <= 2e-6).  The shapes cover
+even and odd N1 (the two c2r kernels), a length with the prime factor 61 (the generic
+odd-radix stage) and a shape at the size limit (N1 = N2 = 512, M * 257 * 512 * K just
+under 2^21 complex floats).
 """
 import numpy as np
 import pytest
@@ -27,7 +30,8 @@ def _noalloc(bb, torch, X, M, N1, N2, K):
 def test_noalloc_c2r_2d_matches_plan_on_two_calls(bb, torch_cuda):
     torch = torch_cuda
     rng = np.random.default_rng(2024)
-    for M, N1, N2, K in [(3, 32, 24, 5), (1, 128, 128, 9)]:
+    for M, N1, N2, K in [(3, 32, 24, 5), (1, 128, 128, 9), (2, 15, 13, 4), (1, 122, 61, 3),
+                         (1, 512, 512, 15)]:
         h = N1 // 2 + 1
         n = M * h * N2 * K
         X = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
