@@ -78,9 +78,11 @@ def newer(target, deps):
 
 def generate_specializations():
     sys.path.insert(0, CSRC)
+    import gen_prime_frags
     import gen_specializations
 
-    return gen_specializations.main(os.path.join(BUILD, 'gen'))
+    frag = gen_prime_frags.main(os.path.join(BUILD, 'gen'))
+    return gen_specializations.main(os.path.join(BUILD, 'gen')) + (frag,)
 
 
 def build(verbose=False, jobs=None):
@@ -89,9 +91,10 @@ def build(verbose=False, jobs=None):
     cuda = cuda_home()
     nvcc = os.path.join(cuda, 'bin', 'nvcc')
     embed_engine()
-    gen_units, rag_units = generate_specializations()
+    gen_units, rag_units, frag_header = generate_specializations()
     headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC)
-               if h.endswith(('.h', '.hpp', '.cuh'))] + [os.path.join(INCLUDE, 'bbfft_gb300.h')]
+               if h.endswith(('.h', '.hpp', '.cuh'))] + [os.path.join(INCLUDE, 'bbfft_gb300.h'),
+                                                        frag_header]
     common_inc = ['-I' + CSRC, '-I' + INCLUDE, '-I' + BUILD, '-I' + os.path.join(BUILD, 'gen'),
                   '-I' + os.path.join(cuda, 'include')]
     jobs_list = []

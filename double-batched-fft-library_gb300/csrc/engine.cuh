@@ -36,6 +36,9 @@
 
 #include "params.h"
 #include "radix.cuh"
+#ifndef GBFFT_NVRTC
+#include "prime_tc.cuh"
+#endif
 
 namespace gbfft {
 
@@ -263,12 +266,79 @@ __device__ __forceinline__ int gen_table_rows(int P) {
     return ((P - 1) / 2 + gen_group - 1) / gen_group * gen_group;
 }
 
+#ifndef GBFFT_NVRTC
+// Float prime radix 17..61 on the tensor cores (prime_tc.cuh): the block's butterflies
+// (Mb * Kb transforms x Nc / P) in groups of 8 per full warp, shared source buffer to
+// shared destination buffer, stage twiddles applied as the inputs are loaded.  The host
+// launches such kernels with a multiple of 32 threads.
+template <int P, class R, int Kind, class IO>
+__device__ __forceinline__ void run_stage_prime_tc(const transform_ctx<R, Kind, IO> &c, int Ns,
+                                                   int src_buf, int dst_buf) {
+    const fft_params &p = c.p;
+    const int nb = p.Nc / P;
+    const int mb = p.Mb;
+    const int nbf = mb * p.Kb * nb;
+    const int ngrp = (nbf + 7) / 8;
+    const int lane = threadIdx.x & 31;
+    const int nwarps = blockDim.x >> 5;
+    const int twstride = p.Nt / (Ns * P);
+    const float2 *tw = static_cast<const float2 *>(p.tw);
+    float2 *sm = c.sm;
+    const int pshift = c.pshift, padd = c.padd, bufe = c.bufe;
+    for (int grp = threadIdx.x >> 5; grp < ngrp; grp += nwarps) {
+        const int q = grp * 8 + (lane >> 2);
+        const bool valid = q < nbf;
+        const int tr = valid ? q / nb : 0;
+        const int b = valid ? q - tr * nb : 0;
+        const int base = (tr / mb) * p.Nc * mb + (tr % mb);
+        const int kk = b % Ns;
+        const int o = b + (b / Ns) * Ns * (P - 1);
+        auto in = [&](int r) {
+            const int i = base + (b + r * nb) * mb;
+            return sm + src_buf * bufe + i + (i >> pshift) * padd;
+        };
+        auto out = [&](int k) {
+            const int i = base + (o + k * Ns) * mb;
+            return sm + dst_buf * bufe + i + (i >> pshift) * padd;
+        };
+        ptc::butterflies8<P>(lane, valid, tw, kk * twstride, in, out);
+    }
+}
+#endif
+
 template <class R, int Kind, class IO>
 __device__ __forceinline__ void run_stage_generic(const transform_ctx<R, Kind, IO> &c, int j,
                                                   int P, int Ns, int src_buf, bool dst_g,
                                                   int dst_buf) {
     using C = cplx<R>;
     const fft_params &p = c.p;
+#ifndef GBFFT_NVRTC
+    if constexpr (sizeof(R) == 4) {
+        if (!dst_g) {
+            switch (P) {
+#define GBFFT_PTC_CASE(Q)                                                                        \
+    case Q:                                                                                      \
+        run_stage_prime_tc<Q>(c, Ns, src_buf, dst_buf);                                          \
+        return;
+                GBFFT_PTC_CASE(17)
+                GBFFT_PTC_CASE(19)
+                GBFFT_PTC_CASE(23)
+                GBFFT_PTC_CASE(29)
+                GBFFT_PTC_CASE(31)
+                GBFFT_PTC_CASE(37)
+                GBFFT_PTC_CASE(41)
+                GBFFT_PTC_CASE(43)
+                GBFFT_PTC_CASE(47)
+                GBFFT_PTC_CASE(53)
+                GBFFT_PTC_CASE(59)
+                GBFFT_PTC_CASE(61)
+#undef GBFFT_PTC_CASE
+            default:
+                break;
+            }
+        }
+    }
+#endif
     const int Nc = p.Nc;
     const int T = p.T;
     const int nb = Nc / P;

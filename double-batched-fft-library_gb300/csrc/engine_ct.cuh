@@ -12,6 +12,7 @@
 #pragma once
 
 #include "engine.cuh"
+#include "prime_tc.cuh"
 
 namespace gbfft {
 
@@ -330,9 +331,45 @@ __device__ __forceinline__ void ct_prime_group(const Ctx &c, int b, int nb, cplx
     });
 }
 
+// Float prime radix as the last stage: the tile's butterflies in groups of 8 per warp on
+// the tensor cores (prime_tc.cuh), in place (a butterfly's outputs overwrite its own
+// inputs when NS * P == NC).  Every full warp of the block takes part; the host launches
+// these tiles with a multiple of 32 threads.
+template <int P, int NS, class Ctx, int NC>
+__device__ __forceinline__ void ct_stage_prime_tc(const Ctx &c) {
+    static_assert(NS * P == NC && Ctx::LIN, "tensor-core prime stage: last stage, scalar layout");
+    constexpr int nb = NC / P;
+    constexpr int twstride = (Ctx::half ? 2 * NC : NC) / NC;
+    const fft_params &p = c.p;
+    const int mb = p.Mb;
+    const int nbf = mb * p.Kb * nb; // butterflies of the tile
+    const int ngrp = (nbf + 7) / 8;
+    const int lane = threadIdx.x & 31;
+    const int nwarps = blockDim.x >> 5;
+    const float2 *tw = static_cast<const float2 *>(p.tw);
+    float2 *sm = c.sm;
+    const int pshift = c.pshift, padd = c.padd;
+    for (int grp = threadIdx.x >> 5; grp < ngrp; grp += nwarps) {
+        const int q = grp * 8 + (lane >> 2);
+        const bool valid = q < nbf;
+        const int tr = valid ? q / nb : 0;
+        const int b = valid ? q - tr * nb : 0;
+        const int base = (tr / mb) * NC * mb + (tr % mb) + b * mb;
+        auto at = [&](int n) {
+            const int i = base + n * (nb * mb);
+            return sm + i + (i >> pshift) * padd;
+        };
+        ptc::butterflies8<P>(lane, valid, tw, b * twstride, at, at);
+    }
+}
+
 template <int P, int NS, class Ctx, class R, int NC, int TT>
 __device__ __forceinline__ void ct_stage_prime(const Ctx &c, int j) {
     using C = cplx<R>;
+    if constexpr (sizeof(R) == 4 && NS * P == NC && ptc::supported(P)) {
+        (void)j;
+        ct_stage_prime_tc<P, NS, Ctx, NC>(c);
+    } else {
     constexpr int nb = NC / P;
     constexpr int H = (P - 1) / 2;
     constexpr int G = sizeof(R) == 4 ? 8 : 4;
@@ -393,6 +430,7 @@ __device__ __forceinline__ void ct_stage_prime(const Ctx &c, int j) {
                 }
             });
         }
+    }
     }
 }
 

@@ -293,9 +293,16 @@ static bool unrolled(int P) { return P == 1 || (P >= 2 && P <= 13) || P == 16; }
 // Generic (non-unrolled) odd radix with the coefficient table of run_stage_generic
 // (engine.cuh): one thread per group of gen_group output pairs of a butterfly.
 static bool table_generic(int P) { return !unrolled(P) && P % 2 == 1 && P <= gen_table_max_p; }
+static bool ptc_supported_host(int P) {
+    return P == 17 || P == 19 || P == 23 || P == 29 || P == 31 || P == 37 || P == 41 || P == 43 ||
+           P == 47 || P == 53 || P == 59 || P == 61;
+}
+// Float prime radices 17..61 run on the tensor cores (prime_tc.cuh): no shared table,
+// and every warp of the block must be full.
+static bool tc_prime(int prec, int P) { return prec == 4 && ptc_supported_host(P); }
 // shared-memory elements the generic stage of radix P needs after the data buffers
-static int gen_shared_elems(int P) {
-    if (unrolled(P)) {
+static int gen_shared_elems(int prec, int P) {
+    if (unrolled(P) || tc_prime(prec, P)) {
         return 0;
     }
     if (P <= gen_table_max_p) {
@@ -1050,7 +1057,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     std::size_t celem = 2 * static_cast<std::size_t>(q.prec);
     int pgen = 0; // generic stages keep their coefficient tables in shared memory
     for (int r : rad) {
-        pgen = std::max(pgen, gen_shared_elems(r));
+        pgen = std::max(pgen, gen_shared_elems(q.prec, r));
     }
     // (compile-time kernels keep their prime coefficients in the code)
     std::size_t const gen_extra = ct ? 0 : static_cast<std::size_t>(pgen) * celem;
@@ -1120,6 +1127,11 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     }
     ps.grid = static_cast<unsigned>(p.m_tiles * k_tiles);
     ps.block = static_cast<unsigned>((Mb / V) * T * Kb);
+    if (!has_cb && std::any_of(rad.begin(), rad.end(), [&](int r) { return tc_prime(q.prec, r); })) {
+        // tensor-core prime stages run on full warps; the extra threads only take part in
+        // the barriers (both engines support threads beyond the tile)
+        ps.block = (ps.block + 31) / 32 * 32;
+    }
     ps.V = V;
     ps.smem = smem;
     ps.inplace_ok = !is_real || Mb >= M;
@@ -1310,7 +1322,7 @@ const char *plan_pass_fixed(int prec, int type, int dir, long long M, long long 
     p.buf_elems = static_cast<int>(last + (last >> best.sh) * best.ad + 1);
     int pgen = 0;
     for (int i = 0; i < L; ++i) {
-        pgen = std::max(pgen, gen_shared_elems(rad[i]));
+        pgen = std::max(pgen, gen_shared_elems(prec, rad[i]));
     }
     smem = static_cast<std::size_t>(nbuf) * p.buf_elems * celem + static_cast<std::size_t>(pgen) * celem;
     int optin = 0;
@@ -1326,6 +1338,12 @@ const char *plan_pass_fixed(int prec, int type, int dir, long long M, long long 
     }
     grid = static_cast<unsigned>(p.m_tiles * k_tiles);
     block = static_cast<unsigned>(Mb * T * Kb);
+    for (int i = 0; i < L; ++i) {
+        if (tc_prime(prec, rad[i])) { // tensor-core prime stages run on full warps
+            block = (block + 31) / 32 * 32;
+            break;
+        }
+    }
     func = ct ? ct->fn : (prec == 4 ? kernel_f32(kind) : kernel_f64(kind));
     if (needs_smem_optin(smem) &&
         cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {

@@ -298,7 +298,7 @@ def test_full_size_round_trip(bb, po, torch_cuda, N):
     torch.cuda.empty_cache()
 
 
-@pytest.mark.parametrize('type', [0, 1])
+@pytest.mark.parametrize('type', [0, 1, 2])
 def test_plans_of_the_ragged_lengths(bb, po, torch_cuda, type):
     """Float plans of every N in {16, 24, ..., 512} (the lengths the ragged tile functions
     cover, incl. the prime factors 17..61), forward and backward, against the oracle in FP64."""
@@ -307,17 +307,62 @@ def test_plans_of_the_ragged_lengths(bb, po, torch_cuda, type):
     for N in range(16, 513, 8):
         M = int(rng.choice([1, 3, 8]))
         K = int(rng.integers(1, 20))
-        for d in ([bb.FORWARD, bb.BACKWARD] if type == 0 else [bb.FORWARD]):
+        for d in ([bb.FORWARD, bb.BACKWARD] if type == 0 else [bb.BACKWARD if type == 2 else bb.FORWARD]):
             cfg = bb.configuration(1, [M, N, K], precision=bb.F32, type=type, direction=d)
+            nin = N // 2 + 1 if type == 2 else N
             nout = N // 2 + 1 if type == 1 else N
             if type == 1:
                 x = rng.standard_normal(M * N * K).astype(np.float32)
             else:
-                x = (rng.standard_normal(M * N * K) + 1j * rng.standard_normal(M * N * K)).astype(np.complex64)
-            out = run(bb, torch, cfg, x, M * nout * K, np.complex64)
-            ref = po.oracle_fft(1, [M, N, K], type, d, x.astype(np.complex128 if type == 0 else np.float64), prec=8)
+                x = (rng.standard_normal(M * nin * K) + 1j * rng.standard_normal(M * nin * K)).astype(np.complex64)
+            out = run(bb, torch, cfg, x, M * nout * K, np.float32 if type == 2 else np.complex64)
+            ref = po.oracle_fft(1, [M, N, K], type, d, x.astype(np.complex128 if type != 1 else np.float64), prec=8)
             e = rel_l2(out, ref)
             assert e <= TOL[4], (N, M, K, d, e)
+
+
+def _largest_prime_factor(n):
+    f, p = 1, 2
+    while n > 1:
+        if n % p == 0:
+            f = p
+            n //= p
+        else:
+            p += 1
+    return f
+
+
+# every length up to 512 with a prime factor 17..61 (the tensor-core prime stages of the
+# float engines), each once as c2c, r2c and c2r
+PRIME_TC_N = [n for n in range(17, 513) if 17 <= _largest_prime_factor(n) <= 61]
+
+
+@pytest.mark.parametrize('type', [0, 1, 2])
+def test_prime_factor_lengths(bb, po, torch_cuda, type):
+    """Float plans of every N <= 512 whose largest prime factor is 17..61 (stages on the
+    tensor cores with split TF32 operands), random double batching, against the oracle in
+    FP64 within the float tolerance."""
+    torch = torch_cuda
+    rng = np.random.default_rng(11 + type)
+    worst = 0.0
+    for N in PRIME_TC_N:
+        M = int(rng.choice([1, 2, 4, 8, 16]))
+        K = int(rng.integers(1, 24))
+        d = bb.BACKWARD if type == 2 else (bb.FORWARD if type == 1 else
+                                           int(rng.choice([bb.FORWARD, bb.BACKWARD])))
+        cfg = bb.configuration(1, [M, N, K], precision=bb.F32, type=type, direction=d)
+        nin = N // 2 + 1 if type == 2 else N
+        nout = N // 2 + 1 if type == 1 else N
+        if type == 1:
+            x = rng.standard_normal(M * nin * K).astype(np.float32)
+        else:
+            x = (rng.standard_normal(M * nin * K) + 1j * rng.standard_normal(M * nin * K)).astype(np.complex64)
+        out = run(bb, torch, cfg, x, M * nout * K, np.float32 if type == 2 else np.complex64)
+        ref = po.oracle_fft(1, [M, N, K], type, d, x.astype(np.complex128 if type != 1 else np.float64), prec=8)
+        e = rel_l2(out, ref)
+        worst = max(worst, e)
+        assert e <= TOL[4], (N, M, K, d, e)
+    print('worst rel-L2', worst)
 
 
 @pytest.mark.parametrize('type,N,M', [(1, 160, 8), (2, 160, 8), (0, 64, 1), (2, 384, 8), (1, 96, 8)])
