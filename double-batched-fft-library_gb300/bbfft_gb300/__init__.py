@@ -19,6 +19,7 @@ F32, F64 = 4, 8
 FORWARD, BACKWARD = -1, 1
 C2C, R2C, C2R = 0, 1, 2
 COMPUTE_NATIVE, COMPUTE_BF16, COMPUTE_SPLIT_BF16, COMPUTE_SPLIT_BF16_3TERM = 0, 1, 2, 3
+COMPUTE_SPLIT_TF32 = 4
 
 STATUS = {
     0: 'SUCCESS', -1: 'BAD_CONFIGURATION', -2: 'INVALID_ARGUMENT', -3: 'CUDA_ERROR',

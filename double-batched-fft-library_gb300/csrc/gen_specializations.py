@@ -77,18 +77,46 @@ def choose_radices(nc):
 BIG_PRIMES = {17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61}
 
 
+def tile_threads(nc, rad, V=1):
+    """Threads per transform of a compile-time tile (same rule as tile_threads() in
+    library.cpp): the count that leaves the fewest thread slots idle over the stages
+    (a stage of nb butterflies runs ceil(nb / T) rounds on T threads), with at most 32
+    complex values per thread (V transforms each) in any stage and at least 4 threads
+    where a stage has 4 butterflies (consecutive threads load consecutive elements of a
+    transform: 32-byte sectors when M = 1); ties go to more threads.  The tensor-core
+    prime stages use every warp of the block and do not count."""
+    nbmax = max([nc // r for r in rad if r not in BIG_PRIMES] + [1])
+    best_t, best_cost = 1, None
+    for t in range(min(4, nbmax), min(nc, 256) + 1):
+        cost, ok = 0, True
+        for r in rad:
+            if r in BIG_PRIMES:
+                continue
+            rounds = -(-(nc // r) // t)
+            if rounds * r * V > 32:
+                ok = False
+                break
+            cost += rounds * t
+        if ok and (best_cost is None or cost <= best_cost):
+            best_t, best_cost = t, cost
+    return best_t
+
+
 def stage_list(nc, kind, ragged=False):
     """Radices incl. the copy stages the host adds, and threads per transform (the rules
-    of make_1d_pass in library.cpp; `ragged`: a pass of a ragged batch)."""
+    of make_1d_pass in library.cpp; `ragged`: a compile-time tile, i.e. a pass of a ragged
+    batch or a plan on a tile kernel)."""
     rad = choose_radices(nc)
     if rad[0] not in UNROLLED:
         rad = [1] + rad
     real = kind != 0
     post = kind == 1
-    if ragged and not post and rad[-1] in BIG_PRIMES:
+    if not post and rad[-1] in BIG_PRIMES:
         rad = rad + [1]
     if real and not post and len(rad) == 1:
         rad = rad + [1]
+    if ragged:
+        return rad, tile_threads(nc, rad)
     pu = max([r for r in rad if r in UNROLLED] + [1])
     T = max(1, nc // pu) if pu > 1 else min(nc, 64)
     ptg = max([r for r in rad if r in BIG_PRIMES] + [0])
@@ -173,8 +201,83 @@ def ragged_entries():
             # the prime stages are scalar
             vw = vector_width(4, rad)
             if vw > 1 and not any(r in BIG_PRIMES for r in rad):
-                out.append((4, kind, nc, T, rad, vw))
+                out.append((4, kind, nc, tile_threads(nc, rad, vw), rad, vw))
     return out
+
+
+def largest_prime_factor(n):
+    return max(prime_factors(n)) if n > 1 else 1
+
+
+def cover_entries():
+    """Compile-time tiles (V = 1) for every other float length N <= 512 whose prime
+    factors are at most 61, each kind: c2c N = 16..512, r2c / c2r even N (complex half
+    length 8..256), r2c / c2r odd N = 17..511.  Lengths with a plan kernel or a ragged
+    tile of their own are left out; longer prime factors stay on the runtime-size engine."""
+    plan = set((k, nc) for (pr, k, nc, T, rad, V, minb) in entries() if pr == 4)
+    rag = set((k, nc) for (pr, k, nc, T, rad, V) in ragged_entries())
+    out = []
+    for kind in KINDS:
+        ncs = range(16, 513) if kind == 0 else (range(8, 257) if kind in (1, 3) else range(17, 512, 2))
+        for nc in ncs:
+            if largest_prime_factor(nc) > 61 or (kind, nc) in plan or (kind, nc) in rag:
+                continue
+            rad, T = stage_list(nc, kind, ragged=True)
+            out.append((4, kind, nc, T, rad, 1))
+    return out
+
+
+COVER_UNIT_KERNELS = 40
+
+
+def cover_units(outdir):
+    """cover_ct_<g>.cu (one plan kernel per cover entry) and the host table lines."""
+    ents = cover_entries()
+    n_units = (len(ents) + COVER_UNIT_KERNELS - 1) // COVER_UNIT_KERNELS
+    groups = [list(range(g, len(ents), n_units)) for g in range(n_units)]
+    units = []
+    for g, idx in enumerate(groups):
+        src = ['// generated by gen_specializations.py: compile-time tiles of the other lengths',
+               '#include "engine_ct.cuh"', '#include "kernels.hpp"', '', 'namespace gbfft {', '']
+        for i in idx:
+            prec, kind, nc, T, rad, V = ents[i]
+            targs = 'float, %d, %d, %d, %d, %s' % (kind, nc, T, V, ', '.join(map(str, rad)))
+            src += ['__global__ void __launch_bounds__(256, 2) cover_ct_%d(const __grid_constant__ fft_params p) {' % i,
+                    '    fft_tile_ct_ragged<%s>(p, blockIdx.x);' % targs, '}', '']
+        src += ['const void *cover_ct_kernel_%d(int i) {' % g, '    switch (i) {']
+        for i in idx:
+            src += ['    case %d:' % i, '        return reinterpret_cast<const void *>(&cover_ct_%d);' % i]
+        src += ['    default:', '        return nullptr;', '    }', '}', '', '} // namespace gbfft', '']
+        fn = os.path.join(outdir, 'cover_ct_%d.cu' % g)
+        write(fn, '\n'.join(src))
+        units.append(fn)
+    host = ['const void *cover_ct_kernel_%d(int i);' % g for g in range(n_units)]
+    host += ['', '// compile-time tile kernels of the other lengths (cover_entries), by table index',
+             'const void *cover_ct_kernel(int i) {',
+             '    switch (i %% %d) {' % n_units]
+    for g in range(n_units):
+        host += ['    case %d:' % g, '        return cover_ct_kernel_%d(i);' % g]
+    host += ['    }', '    return nullptr;', '}', '', 'extern const ct_entry cover_ct_table[] = {']
+    for prec, kind, nc, T, rad, V in ents:
+        host.append('    {%d, %d, %d, %d, %d, %d, {%s}, nullptr, 2},' % (prec, kind, nc, T, V, len(rad), ', '.join(map(str, rad))))
+    host += ['};', 'static const int kCoverSize = %d;' % len(ents), '',
+             'int cover_ct_lookup(int prec, int kind, int nc, int T, const int *rad, int L) {',
+             '    for (int i = 0; i < kCoverSize; ++i) {',
+             '        const ct_entry &e = cover_ct_table[i];',
+             '        if (e.prec != prec || e.kind != kind || e.nc != nc || e.T != T || e.L != L) {',
+             '            continue;',
+             '        }',
+             '        bool same = true;',
+             '        for (int s = 0; s < L; ++s) {',
+             '            same = same && e.rad[s] == rad[s];',
+             '        }',
+             '        if (same) {',
+             '            return i;',
+             '        }',
+             '    }',
+             '    return -1;',
+             '}', '']
+    return units, host
 
 
 def write(fn, text):
@@ -327,14 +430,15 @@ def main(outdir):
               '    return nullptr;',
               '}', '']
     rag_units, rag_host = ragged_units(outdir)
-    index += rag_host + ['} // namespace gbfft', '']
+    cov_units, cov_host = cover_units(outdir)
+    index += rag_host + cov_host + ['} // namespace gbfft', '']
     fn = os.path.join(outdir, 'ct_index.cpp')
     text = '\n'.join(index)
     if not os.path.exists(fn) or open(fn).read() != text:
         with open(fn, 'w') as f:
             f.write(text)
-    return (sorted(os.path.join(outdir, 'kernels_ct_f%d_%s_%d.cu' % (p * 8, KINDS[k], n)) for p, k, n in files),
-            rag_units)
+    return (sorted(os.path.join(outdir, 'kernels_ct_f%d_%s_%d.cu' % (p * 8, KINDS[k], n)) for p, k, n in files)
+            + cov_units, rag_units)
 
 
 if __name__ == '__main__':

@@ -26,6 +26,11 @@ const ct_entry *ct_lookup(int prec, int kind, int nc, int T, int V, const int *r
 // compile-time-size tiles of the persistent ragged kernel: index into ragged_ct_table or -1
 extern const ct_entry ragged_ct_table[];
 int ragged_ct_lookup(int prec, int kind, int nc, int T, int V, const int *rad, int L);
+// compile-time-size tiles (V = 1) of the other float lengths with prime factors <= 61:
+// index into cover_ct_table or -1, and the plan kernel of an index
+extern const ct_entry cover_ct_table[];
+int cover_ct_lookup(int prec, int kind, int nc, int T, const int *rad, int L);
+const void *cover_ct_kernel(int i);
 
 // tensor-core DFT stages (tc.cu)
 const void *tc_kernel(int pieces, int nc);

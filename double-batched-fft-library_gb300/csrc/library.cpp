@@ -586,6 +586,43 @@ static int vector_width(int prec, std::vector<int> const &rad) {
     return v;
 }
 
+// Threads per transform of a compile-time tile (the ragged tiles and the tiles of the
+// other lengths; gen_specializations.py tile_threads() is the same rule): the count that
+// leaves the fewest thread slots idle over the stages (a stage of nb butterflies runs
+// ceil(nb / T) rounds on T threads), with at most 32 complex values per thread (V
+// transforms each) in any stage and at least 4 threads where a stage has 4 butterflies
+// (consecutive threads load consecutive elements: 32-byte sectors when M = 1); ties go to
+// more threads.  The tensor-core prime stages use every warp of the block and do not count.
+static int tile_threads(int nc, const int *rad, int L, int V) {
+    auto counts = [](int r) { return !(r > 16 && ptc_supported_host(r)); };
+    int nbmax = 1;
+    for (int s = 0; s < L; ++s) {
+        if (counts(rad[s])) {
+            nbmax = std::max(nbmax, nc / rad[s]);
+        }
+    }
+    int best_t = 1;
+    long best_cost = -1;
+    for (int t = std::min(4, nbmax); t <= std::min(nc, 256); ++t) {
+        long cost = 0;
+        bool ok = true;
+        for (int s = 0; s < L && ok; ++s) {
+            int const r = rad[s];
+            if (!counts(r)) {
+                continue;
+            }
+            int const rounds = (nc / r + t - 1) / t;
+            ok = rounds * r * V <= 32;
+            cost += static_cast<long>(rounds) * t;
+        }
+        if (ok && (best_cost < 0 || cost <= best_cost)) {
+            best_t = t;
+            best_cost = cost;
+        }
+    }
+    return best_t;
+}
+
 // Shared-memory bank model.  One warp instruction in which every lane moves `w` bytes
 // (8 or 16) is served in wavefronts of 128 / w lanes; within a wavefront a bank serves one
 // 4-byte word at a time, so the cost of a wavefront is the largest number of distinct words
@@ -899,7 +936,11 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     bool post = ps.kind == kind_r2c_half;
     if (q.compute != BBFFT_COMPUTE_NATIVE) {
         // tensor-core DFT stages (tc.cu): fixed tiles of whole transforms
-        int pieces = q.compute == BBFFT_COMPUTE_BF16 ? 1 : q.compute == BBFFT_COMPUTE_SPLIT_BF16_3TERM ? 2 : 3;
+        // BF16 pieces per operand; 0 selects the split-TF32 kernels
+        int pieces = q.compute == BBFFT_COMPUTE_BF16               ? 1
+                     : q.compute == BBFFT_COMPUTE_SPLIT_BF16_3TERM ? 2
+                     : q.compute == BBFFT_COMPUTE_SPLIT_TF32       ? 0
+                                                                   : 3;
         fft_params &p = ps.p;
         p.M = 1;
         p.K = q.K;
@@ -1003,7 +1044,10 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     // compile-time-size tile functions of the ragged set (float, V = 1): the tiles of
     // ragged batches, and plans of lengths without a compile-time plan kernel
     int ragged_vid = -1;
+    int cover_id = -1;
     if (!has_cb && !ct && q.prec == 4) {
+        // compile-time tiles choose their own threads per transform (tile_threads)
+        int const Tt = reqT > 0 ? T : tile_threads(Nc, rad.data(), L, 1);
         int vw = vector_width(q.prec, rad);
         if (reqV > 0) {
             vw = std::min(vw, reqV);
@@ -1011,15 +1055,30 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         bool v_ok = !q.force_v1 && vw > 1 && M % vw == 0 && q.is1 % vw == 0 && q.os1 % vw == 0 &&
                     q.is2 % vw == 0 && q.os2 % vw == 0;
         if (v_ok) {
-            ragged_vid = ragged_ct_lookup(q.prec, ps.kind, Nc, T, vw, rad.data(), L);
+            int const Tv = reqT > 0 ? T : tile_threads(Nc, rad.data(), L, vw);
+            ragged_vid = ragged_ct_lookup(q.prec, ps.kind, Nc, Tv, vw, rad.data(), L);
             V = ragged_vid >= 0 ? vw : 1;
+            if (ragged_vid >= 0) {
+                T = Tv;
+            }
         }
         if (ragged_vid < 0) {
-            ragged_vid = ragged_ct_lookup(q.prec, ps.kind, Nc, T, 1, rad.data(), L);
+            ragged_vid = ragged_ct_lookup(q.prec, ps.kind, Nc, Tt, 1, rad.data(), L);
             V = 1;
+            if (ragged_vid >= 0) {
+                T = Tt;
+            }
         }
         if (ragged_vid >= 0) {
             ct = &ragged_ct_table[ragged_vid];
+        } else if (!q.runtime_only) {
+            // plans of the other lengths (not ragged items: the persistent kernel cannot
+            // call these tiles, and the runtime engine needs its own blocking)
+            cover_id = cover_ct_lookup(q.prec, ps.kind, Nc, Tt, rad.data(), L);
+            if (cover_id >= 0) {
+                ct = &cover_ct_table[cover_id];
+                T = Tt;
+            }
         }
     }
     int const max_block = q.max_block > 0 ? q.max_block : (ct ? 256 : 512);
@@ -1157,6 +1216,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     if (!has_cb) {
         ps.func = (ct && ct->fn) ? ct->fn
                   : ragged_vid >= 0 ? ragged_plan_kernel(ragged_vid)
+                  : cover_id >= 0   ? cover_ct_kernel(cover_id)
                                     : (q.prec == 4 ? kernel_f32(ps.kind) : kernel_f64(ps.kind));
         ps.specialized = ct != nullptr;
         ps.min_blocks = ct ? ct->minb : 0; // (+ 10: paired c2r variant)
@@ -1398,7 +1458,7 @@ static void validate(bbfft_configuration const &cfg) {
     }
     if (cfg.compute != BBFFT_COMPUTE_NATIVE) {
         bool ok = cfg.compute == BBFFT_COMPUTE_BF16 || cfg.compute == BBFFT_COMPUTE_SPLIT_BF16 ||
-                  cfg.compute == BBFFT_COMPUTE_SPLIT_BF16_3TERM;
+                  cfg.compute == BBFFT_COMPUTE_SPLIT_BF16_3TERM || cfg.compute == BBFFT_COMPUTE_SPLIT_TF32;
         std::size_t N = cfg.shape[1];
         ok = ok && cfg.dim == 1 && cfg.type == BBFFT_C2C && cfg.precision == BBFFT_PRECISION_F32 &&
              (N == 64 || N == 256 || N == 512) && cfg.shape[0] == 1 && cfg.istride[1] == 1 &&

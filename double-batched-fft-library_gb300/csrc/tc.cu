@@ -15,6 +15,7 @@
 // The reference has no tensor-core path.
 #include "engine.cuh"
 #include "kernels.hpp"
+#include "prime_tc.cuh"
 
 #include <cuda_bf16.h>
 
@@ -228,6 +229,89 @@ __device__ __forceinline__ void stage_last(const float2 *src, float2 *out, int N
     }
 }
 
+// One radix-P stage (P = 16 or 32) on the tensor cores with split TF32 operands
+// (prime_tc.cuh: the pair sums and differences of each butterfly against the cosine and
+// sine matrices, two TF32 pieces per operand, three products): src -> dst, all transforms
+// of the tile, eight butterflies per warp at a time.
+template <int P, int NC>
+__device__ __forceinline__ void stage_tf32(const float2 *src, float2 *dst, int Ns, const float2 *tw,
+                                           int tiles) {
+    constexpr int nb = NC / P;
+    const int lane = threadIdx.x & 31;
+    const int ngrp = tiles * nb / 8; // tiles * nb = kElems / P, a multiple of 8
+    const int twstride = NC / (Ns * P);
+    for (int grp = threadIdx.x >> 5; grp < ngrp; grp += kThreads / 32) {
+        const int q = grp * 8 + (lane >> 2);
+        const int t = q / nb, b = q % nb;
+        const int kk = b % Ns;
+        const int o = b + (b / Ns) * Ns * (P - 1);
+        auto in = [&](int r) { return src + pad<NC>(t * NC + b + r * nb); };
+        auto out = [&](int k) { return dst + pad<NC>(t * NC + o + k * Ns); };
+        ptc::butterflies8<P>(lane, true, tw, kk * twstride, in, out);
+    }
+}
+
+// contiguous tile in shared memory -> global (16-byte stores), conjugated for backward
+template <int NC>
+__device__ __forceinline__ void store_tile(const float2 *buf, float2 *yt, long long nt, bool conj_out) {
+    for (int i = threadIdx.x; i < kElems / 2; i += kThreads) {
+        if (2 * i < nt * NC) {
+            float2 a = buf[pad<NC>(2 * i)], b = buf[pad<NC>(2 * i + 1)];
+            if (conj_out) {
+                a.y = -a.y;
+                b.y = -b.y;
+            }
+            reinterpret_cast<float4 *>(yt)[i] = make_float4(a.x, a.y, b.x, b.y);
+        }
+    }
+}
+
+// contiguous tile global -> shared (16-byte loads), conjugated for backward
+template <int NC>
+__device__ __forceinline__ void load_tile(const float2 *x, float2 *buf, long long nt, bool conj_in) {
+    for (int i = threadIdx.x; i < kElems / 2; i += kThreads) {
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (2 * i < nt * NC) {
+            v = reinterpret_cast<const float4 *>(x)[i];
+        }
+        if (conj_in) {
+            v.y = -v.y;
+            v.w = -v.w;
+        }
+        buf[pad<NC>(2 * i)] = mk<float>(v.x, v.y);
+        buf[pad<NC>(2 * i + 1)] = mk<float>(v.z, v.w);
+    }
+}
+
+// Split-TF32 form, c2c float, M = 1, packed: 64 = 32 x 2, 256 = 16 x 16, 512 = 32 x 16, the
+// radix-16 / 32 stages on the tensor cores, the radix-2 stage on the CUDA cores.
+template <int NC> __global__ void __launch_bounds__(kThreads, 3) fft_tc32_kernel(const __grid_constant__ fft_params p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int tiles = kElems / NC;
+    float2 *buf0 = reinterpret_cast<float2 *>(smem_raw);
+    float2 *buf1 = buf0 + kBufElems;
+    const float2 *tw = static_cast<const float2 *>(p.tw);
+    const bool conj_in = p.flags & flag_conj_in, conj_out = p.flags & flag_conj_out;
+    const long long t0 = static_cast<long long>(blockIdx.x) * tiles;
+    const long long nt = (p.K - t0) < tiles ? (p.K - t0) : tiles;
+    const float2 *x = static_cast<const float2 *>(p.in) + t0 * NC;
+    float2 *y = static_cast<float2 *>(p.out);
+    load_tile<NC>(x, buf0, nt, conj_in);
+    __syncthreads();
+    if constexpr (NC == 64) {
+        stage_tf32<32, NC>(buf0, buf1, 1, tw, tiles);
+        __syncthreads();
+        stage_last<2, NC>(buf1, y, 32, tw, tiles, t0, p.K, conj_out);
+    } else {
+        constexpr int P0 = NC == 256 ? 16 : 32;
+        stage_tf32<P0, NC>(buf0, buf1, 1, tw, tiles);
+        __syncthreads();
+        stage_tf32<16, NC>(buf1, buf0, P0, tw, tiles);
+        __syncthreads();
+        store_tile<NC>(buf0, y + t0 * NC, nt, conj_out);
+    }
+}
+
 // c2c float, M = 1, packed: tiles of kElems / NC transforms per CTA.
 template <int PIECES, int NC> __global__ void __launch_bounds__(kThreads, 3) fft_tc_kernel(const __grid_constant__ fft_params p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -301,6 +385,17 @@ const void *tc_kernel(int pieces, int nc) {
     GBFFT_TC(3, 256)
     GBFFT_TC(3, 512)
 #undef GBFFT_TC
+    // pieces == 0: the split-TF32 form
+    if (pieces == 0) {
+        switch (nc) {
+        case 64:
+            return reinterpret_cast<const void *>(&tc::fft_tc32_kernel<64>);
+        case 256:
+            return reinterpret_cast<const void *>(&tc::fft_tc32_kernel<256>);
+        case 512:
+            return reinterpret_cast<const void *>(&tc::fft_tc32_kernel<512>);
+        }
+    }
     return nullptr;
 }
 

@@ -69,6 +69,9 @@ typedef enum bbfft_status {
 #define BBFFT_COMPUTE_BF16 1       /* tensor-core radix-16 stages, BF16 operands, FP32 accumulate */
 #define BBFFT_COMPUTE_SPLIT_BF16 2 /* operands split in 3 BF16 pieces, 6 product terms (~FP32) */
 #define BBFFT_COMPUTE_SPLIT_BF16_3TERM 3 /* operands split in 2 BF16 pieces, 3 product terms */
+#define BBFFT_COMPUTE_SPLIT_TF32 4 /* radix-16 / 32 stages as TF32 products of the pair sums and
+                                    * differences, operands in 2 TF32 pieces, 3 product terms
+                                    * (~FP32) */
 /* The tensor-core modes apply to 1d c2c float plans with N in {64, 256, 512}, M = 1 and the
  * packed layout; other configurations reject them with BBFFT_BAD_CONFIGURATION. */
 

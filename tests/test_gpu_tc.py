@@ -1,8 +1,10 @@
 """Tensor-core DFT stages (compute modes of c2c float plans, N in {64, 256, 512}).
 
 Inputs follow the benchmark's tensor-core workload: iid N(0,1) complex values with a 1e-3
-fraction scaled by 1e4.  rel-L2 against the FP64 DFT: the 6-term split-BF16 form must meet
-the benchmark spec's 1e-6; the 3-term and plain BF16 forms are reported with looser bounds."""
+fraction scaled by 1e4.  rel-L2 against the FP64 DFT: the 3-term split-TF32 form (two TF32
+pieces of about 11 bits each per operand) and the 6-term split-BF16 form (three BF16 pieces)
+must meet 1e-6.  The 3-term split-BF16 form keeps two BF16 pieces (16 significant bits per
+operand), so its error is about 4e-6 and it is held to 1e-5; plain BF16 to 2e-2."""
 import numpy as np
 import pytest
 
@@ -10,7 +12,8 @@ from gpu_helpers import rel_l2, run
 
 pytestmark = pytest.mark.gpu
 
-MODES = {'native': (0, 2e-6), 'bf16': (1, 2e-2), 'split6': (2, 1e-6), 'split3': (3, 1e-4)}
+MODES = {'native': (0, 2e-6), 'bf16': (1, 2e-2), 'split6': (2, 1e-6), 'split3': (3, 1e-5),
+         'split_tf32': (4, 1e-6)}
 
 
 def tc_input(N, K, seed):
@@ -37,11 +40,13 @@ def test_tensor_core_modes_accuracy(bb, po, torch_cuda, N, direction):
     print('N=%d dir=%d rel-L2 %s' % (N, direction, {k: '%.2e' % v for k, v in errs.items()}))
 
 
-def test_tensor_core_mode_in_place(bb, po, torch_cuda):
+@pytest.mark.parametrize('mode', [2, 4])
+@pytest.mark.parametrize('N', [64, 256, 512])
+def test_tensor_core_mode_in_place(bb, po, torch_cuda, mode, N):
     torch = torch_cuda
-    N, K = 256, 300
+    K = 300
     x = tc_input(N, K, 1)
-    cfg = bb.configuration(1, [1, N, K], precision=bb.F32, compute=2)
+    cfg = bb.configuration(1, [1, N, K], precision=bb.F32, compute=mode)
     out = run(bb, torch, cfg, x, N * K, np.complex64, inplace=True)
     ref = po.dft64(1, [1, N, K], po.C2C, -1, x.astype(np.complex128).reshape(K, N, 1))
     assert rel_l2(out.reshape(ref.shape), ref) <= 1e-6
