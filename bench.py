@@ -888,10 +888,12 @@ def run_e2e(bb, torch, plans, prec, sptr, stream, args):
 
 def run_profile(args):
     """Launches for an ncu capture, no timing: `step` runs every plan of one benchmark step
-    once (28 launches); `case` runs one plan once (KIND:N, KIND in r2c / c2r, float32,
-    M=8, 1 GiB real input -- or c2c:N[:FORM] with M=1, K=2^20, FORM one of native, bf16,
-    split3, split6 for the tensor-core stages); `ragged` runs the ragged batch once in
-    the class form (one kernel per tile function)."""
+    once (28 launches); `case` runs one plan per comma-separated spec
+    KIND:N[:FORM[:M[:PREC]]] once (KIND c2c / r2c / c2r; FORM native, bf16, split3, split6
+    or tf32 for the tensor-core forms of c2c; M default 1 for c2c, 8 otherwise; PREC 4 or
+    8 bytes; K sized for --profile-bytes of input, default 1 GiB, or K = 2^20 for c2c
+    with M = 1); `ragged` runs the ragged batch once in the class form (one kernel per tile
+    function)."""
     import torch
 
     import bbfft_gb300 as bb
@@ -909,32 +911,44 @@ def run_profile(args):
         print('profiled ragged batch, units:', r.info().num_units)
         return
     forms = {'native': bb.COMPUTE_NATIVE, 'bf16': bb.COMPUTE_BF16,
-             'split3': bb.COMPUTE_SPLIT_BF16_3TERM, 'split6': bb.COMPUTE_SPLIT_BF16}
+             'split3': bb.COMPUTE_SPLIT_BF16_3TERM, 'split6': bb.COMPUTE_SPLIT_BF16,
+             'tf32': bb.COMPUTE_SPLIT_TF32}
     if args.profile == 'step':
-        cases = [(t, N, 'native') for N in SWEEP_N for t in ('r2c', 'c2r')]
+        cases = [('r2c' if i % 2 == 0 else 'c2r', N, 'native', M_BATCH, 4)
+                 for N in SWEEP_N for i in range(2)]
     else:
-        f = args.profile_case.split(':')
-        cases = [(f[0], int(f[1]), f[2] if len(f) > 2 else 'native')]
+        cases = []
+        for spec in args.profile_case.split(','):
+            f = spec.split(':')
+            kind, N = f[0], int(f[1])
+            form = f[2] if len(f) > 2 and f[2] else 'native'
+            M = int(f[3]) if len(f) > 3 else (1 if kind == 'c2c' else M_BATCH)
+            prec = int(f[4]) if len(f) > 4 else 4
+            cases.append((kind, N, form, M, prec))
     cfgs = []
-    for kind, N, form in cases:
+    for kind, N, form, M, prec in cases:
+        words = prec // 4  # floats per real
         if kind == 'c2c':
-            cfg = bb.configuration(1, [1, N, 1 << 20], precision=bb.F32, compute=forms[form])
-            nin = nout = 2 * N * (1 << 20)
-        elif kind == 'r2c':
-            K = k_for(N, 4)
-            cfg = bb.configuration(1, [M_BATCH, N, K], precision=bb.F32, type=bb.R2C)
-            nin, nout = M_BATCH * N * K, 2 * M_BATCH * (N // 2 + 1) * K
-        elif kind == 'c2r':
-            K = k_for(N, 4)
-            cfg = bb.configuration(1, [M_BATCH, N, K], precision=bb.F32, type=bb.C2R,
-                                   direction=bb.BACKWARD)
-            nin, nout = 2 * M_BATCH * (N // 2 + 1) * K, M_BATCH * N * K
+            K = (1 << 20) if (M == 1 and args.profile_bytes is None) else \
+                (args.profile_bytes or REAL_BYTES) // (M * N * 2 * prec)
+            cfg = bb.configuration(1, [M, N, K], precision=prec, compute=forms[form])
+            nin = nout = 2 * M * N * K * words
+        elif kind in ('r2c', 'c2r'):
+            K = (args.profile_bytes or REAL_BYTES) // (prec * M * N)
+            if kind == 'r2c':
+                cfg = bb.configuration(1, [M, N, K], precision=prec, type=bb.R2C)
+                nin, nout = M * N * K * words, 2 * M * (N // 2 + 1) * K * words
+            else:
+                cfg = bb.configuration(1, [M, N, K], precision=prec, type=bb.C2R,
+                                       direction=bb.BACKWARD)
+                nin, nout = 2 * M * (N // 2 + 1) * K * words, M * N * K * words
         else:
             raise SystemExit('unknown profile case ' + kind)
         cfgs.append((cfg, nin, nout))
     # buffers sized from the largest input / output extent (in floats) of the cases
     x = torch.randn(max(c[1] for c in cfgs), device='cuda')
     y = torch.empty(max(c[2] for c in cfgs), device='cuda')
+    assert x.numel() * 4 <= (6 << 30), 'profile cases hold a few GB at most'
     for cfg, nin, nout in cfgs:
         assert nin <= x.numel() and nout <= y.numel()
         plan = bb.Plan(cfg, stream=stream)
@@ -956,6 +970,8 @@ def main():
                     help='comma-separated secondary legs to run (default: all): ' + ','.join(LEGS))
     ap.add_argument('--profile', choices=['step', 'case', 'ragged'], help='launches for an ncu capture')
     ap.add_argument('--profile-case', default='c2r:160')
+    ap.add_argument('--profile-bytes', type=int, default=None,
+                    help='input bytes of each --profile case plan (default 1 GiB)')
     args = ap.parse_args()
     if args.profile:
         run_profile(args)

@@ -17,7 +17,9 @@ CSRC = os.path.join(HERE, 'csrc')
 REPO = os.path.dirname(HERE)
 INCLUDE = os.path.join(REPO, 'include')
 OUTDIR = os.path.join(HERE, 'bbfft_gb300', '_lib')
-BUILD = os.path.join(HERE, '_build')
+# object files and generated sources (BBFFT_GB300_BUILD_DIR moves them, e.g. out of a tree
+# that is copied elsewhere)
+BUILD = os.environ.get('BBFFT_GB300_BUILD_DIR') or os.path.join(HERE, '_build')
 LIB = os.path.join(OUTDIR, 'libbbfft_gb300.so')
 # throughput probes for the benchmark's roofline denominators (not part of the library)
 PROBES_SRC = os.path.join(CSRC, 'peak_probes.cu')

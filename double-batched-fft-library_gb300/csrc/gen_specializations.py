@@ -84,22 +84,28 @@ def tile_threads(nc, rad, V=1):
     complex values per thread (V transforms each) in any stage and at least 4 threads
     where a stage has 4 butterflies (consecutive threads load consecutive elements of a
     transform: 32-byte sectors when M = 1); ties go to more threads.  The tensor-core
-    prime stages use every warp of the block and do not count."""
+    prime stages use every warp of the block and do not count, but with one of them T is
+    at most 4 x its butterflies per transform where possible, so that a block of 256
+    threads holds at least 64 of its butterflies (8 per warp)."""
     nbmax = max([nc // r for r in rad if r not in BIG_PRIMES] + [1])
-    best_t, best_cost = 1, None
-    for t in range(min(4, nbmax), min(nc, 256) + 1):
-        cost, ok = 0, True
-        for r in rad:
-            if r in BIG_PRIMES:
-                continue
-            rounds = -(-(nc // r) // t)
-            if rounds * r * V > 32:
-                ok = False
-                break
-            cost += rounds * t
-        if ok and (best_cost is None or cost <= best_cost):
-            best_t, best_cost = t, cost
-    return best_t
+    tcap = min([4 * (nc // r) for r in rad if r in BIG_PRIMES] + [256])
+    for hi in (min(nc, 256, tcap), min(nc, 256)):
+        best_t, best_cost = None, None
+        for t in range(min(4, nbmax), hi + 1):
+            cost, ok = 0, True
+            for r in rad:
+                if r in BIG_PRIMES:
+                    continue
+                rounds = -(-(nc // r) // t)
+                if rounds * r * V > 32:
+                    ok = False
+                    break
+                cost += rounds * t
+            if ok and (best_cost is None or cost <= best_cost):
+                best_t, best_cost = t, cost
+        if best_t is not None:
+            return best_t
+    return 1
 
 
 def stage_list(nc, kind, ragged=False):
@@ -243,6 +249,7 @@ def cover_units(outdir):
             prec, kind, nc, T, rad, V = ents[i]
             targs = 'float, %d, %d, %d, %d, %s' % (kind, nc, T, V, ', '.join(map(str, rad)))
             src += ['__global__ void __launch_bounds__(256, 2) cover_ct_%d(const __grid_constant__ fft_params p) {' % i,
+                    '    pdl_prologue();',
                     '    fft_tile_ct_ragged<%s>(p, blockIdx.x);' % targs, '}', '']
         src += ['const void *cover_ct_kernel_%d(int i) {' % g, '    switch (i) {']
         for i in idx:
@@ -316,6 +323,7 @@ def ragged_units(outdir):
                     '    fft_tile_ct_ragged<%s>(s_p, un.y);' % targs,
                     '}', '',
                     '__global__ void __launch_bounds__(256, 2) plan_ct_%d(const __grid_constant__ fft_params p) {' % i,
+                    '    pdl_prologue();',
                     '    fft_tile_ct_ragged<%s>(p, blockIdx.x);' % targs,
                     '}', '']
         for kname in ('ragged_class_ct', 'plan_ct'):
@@ -391,6 +399,7 @@ def main(outdir):
                '#include "engine_ct.cuh"', '#include "kernels.hpp"', '', 'namespace gbfft {', '',
                'template <class R, int Kind, int NC, int TT, int V, int MINB, int... Ps>',
                '__global__ void __launch_bounds__(256, MINB % 10) fft_kernel_ct(const __grid_constant__ fft_params p) {',
+               '    pdl_prologue();',
                '    fft_tile_ct<R, Kind, NC, TT, V, (MINB >= 10), Ps...>(p);', '}', '',
                'extern const ct_entry %s[] = {' % name]
         for nc, T, rad, V, minb in lst:

@@ -298,11 +298,13 @@ static bool ptc_supported_host(int P) {
            P == 47 || P == 53 || P == 59 || P == 61;
 }
 // Float prime radices 17..61 run on the tensor cores (prime_tc.cuh): no shared table,
-// and every warp of the block must be full.
+// and every warp of the block must be full.  NVRTC kernels (user callbacks) keep the
+// CUDA-core stage and its table.
 static bool tc_prime(int prec, int P) { return prec == 4 && ptc_supported_host(P); }
 // shared-memory elements the generic stage of radix P needs after the data buffers
-static int gen_shared_elems(int prec, int P) {
-    if (unrolled(P) || tc_prime(prec, P)) {
+// (`tc_ok`: the kernel has the tensor-core stages, i.e. it is not an NVRTC kernel)
+static int gen_shared_elems(int prec, int P, bool tc_ok) {
+    if (unrolled(P) || (tc_ok && tc_prime(prec, P))) {
         return 0;
     }
     if (P <= gen_table_max_p) {
@@ -592,35 +594,46 @@ static int vector_width(int prec, std::vector<int> const &rad) {
 // ceil(nb / T) rounds on T threads), with at most 32 complex values per thread (V
 // transforms each) in any stage and at least 4 threads where a stage has 4 butterflies
 // (consecutive threads load consecutive elements: 32-byte sectors when M = 1); ties go to
-// more threads.  The tensor-core prime stages use every warp of the block and do not count.
+// more threads.  The tensor-core prime stages use every warp of the block and do not count,
+// but with one of them T is at most 4 x its butterflies per transform where possible, so
+// that a block of 256 threads holds at least 64 of its butterflies (8 per warp).
 static int tile_threads(int nc, const int *rad, int L, int V) {
     auto counts = [](int r) { return !(r > 16 && ptc_supported_host(r)); };
     int nbmax = 1;
+    int tcap = 256;
     for (int s = 0; s < L; ++s) {
         if (counts(rad[s])) {
             nbmax = std::max(nbmax, nc / rad[s]);
+        } else {
+            tcap = std::min(tcap, 4 * (nc / rad[s]));
         }
     }
-    int best_t = 1;
-    long best_cost = -1;
-    for (int t = std::min(4, nbmax); t <= std::min(nc, 256); ++t) {
-        long cost = 0;
-        bool ok = true;
-        for (int s = 0; s < L && ok; ++s) {
-            int const r = rad[s];
-            if (!counts(r)) {
-                continue;
+    int const his[2] = {std::min({nc, 256, tcap}), std::min(nc, 256)};
+    for (int hi : his) {
+        int best_t = -1;
+        long best_cost = -1;
+        for (int t = std::min(4, nbmax); t <= hi; ++t) {
+            long cost = 0;
+            bool ok = true;
+            for (int s = 0; s < L && ok; ++s) {
+                int const r = rad[s];
+                if (!counts(r)) {
+                    continue;
+                }
+                int const rounds = (nc / r + t - 1) / t;
+                ok = rounds * r * V <= 32;
+                cost += static_cast<long>(rounds) * t;
             }
-            int const rounds = (nc / r + t - 1) / t;
-            ok = rounds * r * V <= 32;
-            cost += static_cast<long>(rounds) * t;
+            if (ok && (best_cost < 0 || cost <= best_cost)) {
+                best_t = t;
+                best_cost = cost;
+            }
         }
-        if (ok && (best_cost < 0 || cost <= best_cost)) {
-            best_t = t;
-            best_cost = cost;
+        if (best_t > 0) {
+            return best_t;
         }
     }
-    return best_t;
+    return 1;
 }
 
 // Shared-memory bank model.  One warp instruction in which every lane moves `w` bytes
@@ -1116,7 +1129,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     std::size_t celem = 2 * static_cast<std::size_t>(q.prec);
     int pgen = 0; // generic stages keep their coefficient tables in shared memory
     for (int r : rad) {
-        pgen = std::max(pgen, gen_shared_elems(q.prec, r));
+        pgen = std::max(pgen, gen_shared_elems(q.prec, r, !has_cb));
     }
     // (compile-time kernels keep their prime coefficients in the code)
     std::size_t const gen_extra = ct ? 0 : static_cast<std::size_t>(pgen) * celem;
@@ -1382,7 +1395,7 @@ const char *plan_pass_fixed(int prec, int type, int dir, long long M, long long 
     p.buf_elems = static_cast<int>(last + (last >> best.sh) * best.ad + 1);
     int pgen = 0;
     for (int i = 0; i < L; ++i) {
-        pgen = std::max(pgen, gen_shared_elems(prec, rad[i]));
+        pgen = std::max(pgen, gen_shared_elems(prec, rad[i], true));
     }
     smem = static_cast<std::size_t>(nbuf) * p.buf_elems * celem + static_cast<std::size_t>(pgen) * celem;
     int optin = 0;
@@ -1671,6 +1684,16 @@ static void make_plan_impl(bbfft_configuration const &cfg, cudaStream_t stream,
     }
 }
 
+// Programmatic dependent launch of the plan kernels (all of them call pdl_prologue);
+// BBFFT_GB300_PDL=0 turns it off.
+static bool pdl_enabled() {
+    static const bool on = [] {
+        const char *e = std::getenv("BBFFT_GB300_PDL");
+        return !(e && std::strcmp(e, "0") == 0);
+    }();
+    return on;
+}
+
 static void execute_impl(bbfft_plan_s &plan, const void *in, void *out, cudaStream_t stream) {
     if (in == out && !plan.inplace_ok) {
         bad_config("The plan does not support in-place transform on the current device. Please "
@@ -1742,7 +1765,24 @@ static void execute_impl(bbfft_plan_s &plan, const void *in, void *out, cudaStre
             p.flags &= ~flag_vec_out;
         }
         void *args[] = {&p};
-        cudaError_t e = cudaLaunchKernel(ps.func, dim3(ps.grid), dim3(ps.block), args, ps.smem, stream);
+        cudaError_t e;
+        if (!ps.mod && pdl_enabled()) {
+            // programmatic dependent launch: the kernel waits for the previous kernel of the
+            // stream itself (pdl_prologue), so its launch may overlap that kernel's tail
+            cudaLaunchConfig_t lc = {};
+            lc.gridDim = dim3(ps.grid);
+            lc.blockDim = dim3(ps.block);
+            lc.dynamicSmemBytes = ps.smem;
+            lc.stream = stream;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            attr[0].val.programmaticStreamSerializationAllowed = 1;
+            lc.attrs = attr;
+            lc.numAttrs = 1;
+            e = cudaLaunchKernelExC(&lc, ps.func, args);
+        } else {
+            e = cudaLaunchKernel(ps.func, dim3(ps.grid), dim3(ps.block), args, ps.smem, stream);
+        }
         if (e != cudaSuccess) {
             throw status_error(BBFFT_CUDA_ERROR,
                                std::string("kernel launch failed: ") + cudaGetErrorString(e));
