@@ -697,7 +697,15 @@ def leg_spectral(bb, torch, stream, steps, warmup):
     for _ in range(warmup):
         step()
     ms = event_time(torch, stream, step, max(steps, 3))
-    return {'ms_fwd_bwd': round(ms, 3), 'shape': 'r2c/c2r 128x128, K=2048, modes 32x32, f32'}
+    # four 2d transforms per step (r2c and c2r forward, their adjoints backward), each one
+    # read and one write of a real (128x128) and a half-spectrum (65x128) tensor of K images
+    K = 64 * 32
+    b = 4 * K * (128 * 128 * 4 + 65 * 128 * 8)
+    return {'ms_fwd_bwd': round(ms, 3), 'gbs_transforms': round(b / ms / 1e6, 1),
+            'transform_bytes': b,
+            'note': 'bytes of the four 2d transforms (one read + one write each); the mode '
+                    'multiply, slicing and zero fill run as torch ops in the same time',
+            'shape': 'r2c/c2r 128x128, K=2048, modes 32x32, f32'}
 
 
 def leg_tft(bb, torch, stream, hbm_peak, steps, warmup):

@@ -1440,6 +1440,13 @@ struct bbfft_plan_s {
     std::shared_ptr<gbfft::device_buffer> packed_in, packed_out;
     bool inplace_ok = true;
     bool jit = false;
+    // nd plans whose intermediate tensor does not fit in a share of the L2 cache run slab by
+    // slab along the K mode: every pass over one slab of slab_k transforms, then the next
+    // slab, so that the intermediate stays in L2 between the passes (0: one slab)
+    long long slab_k = 0;
+    long long slab_count = 0;                // slabs of slab_k transforms
+    std::vector<gbfft::pass> tail_passes;    // passes of a last, shorter slab (if any)
+    std::size_t slab_in_bytes = 0, slab_out_bytes = 0; // pointer advance per slab
 };
 
 namespace gbfft {
@@ -1622,7 +1629,6 @@ static void make_plan_impl(bbfft_configuration const &cfg, cudaStream_t stream,
             q.load_fn = i == 0 ? cfg.load_function : nullptr;
             q.store_fn = i + 1 == order.size() ? cfg.store_function : nullptr;
         }
-        plan.passes.push_back(make_1d_pass(q, plan.device, cache));
     }
     plan.jit = has_cb;
     // temporary buffer if the input is larger than the output (nd_fft.hpp:114-125)
@@ -1635,13 +1641,52 @@ static void make_plan_impl(bbfft_configuration const &cfg, cudaStream_t stream,
     std::size_t const *ost = strided_nd ? pos.data() : adjoint ? cfg.istride : cfg.ostride;
     std::size_t isize = ist[dim + 1] * cfg.shape[dim + 1] * (in_real ? real_b : cplx_b);
     std::size_t osize = ost[dim + 1] * cfg.shape[dim + 1] * (out_real ? real_b : cplx_b);
+    // L2-resident chaining (no counterpart in the reference, which runs each pass over the
+    // whole tensor, nd_fft.hpp:140-152): when the intermediate tensor is larger than a
+    // quarter of the L2 cache, the passes run slab by slab along K, so the intermediate
+    // written by one pass is still in L2 when the next pass reads it and HBM sees about one
+    // read of the input and one write of the output.  Not with callbacks (their offsets are
+    // relative to the whole tensor) or custom layouts (packed copies).
+    long long const Kimg = static_cast<long long>(cfg.shape[dim + 1]);
+    std::size_t const inter_per_k = std::max(isize, osize) / static_cast<std::size_t>(Kimg);
+    int l2 = 0;
+    GB_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, plan.device));
+    std::size_t const budget = static_cast<std::size_t>(l2) / 4;
+    long long slab_k = 0;
+    if (!has_cb && !strided_nd && budget > 0 && inter_per_k * Kimg > budget) {
+        slab_k = std::max<long long>(1, static_cast<long long>(budget / inter_per_k));
+        if (slab_k >= Kimg) {
+            slab_k = 0;
+        }
+    }
+    auto make_passes = [&](long long kk, std::vector<pass> &out) {
+        for (pass_request q : order) {
+            q.K = q.K / Kimg * kk; // the K mode of every pass is (outer modes) x Kimg
+            out.push_back(make_1d_pass(q, plan.device, cache));
+        }
+    };
+    make_passes(slab_k > 0 ? slab_k : Kimg, plan.passes);
+    if (slab_k > 0) {
+        plan.slab_k = slab_k;
+        plan.slab_count = Kimg / slab_k;
+        plan.slab_in_bytes = ist[dim + 1] * slab_k * (in_real ? real_b : cplx_b);
+        plan.slab_out_bytes = ost[dim + 1] * slab_k * (out_real ? real_b : cplx_b);
+        if (Kimg % slab_k != 0) {
+            make_passes(Kimg % slab_k, plan.tail_passes);
+        }
+        // a separate temporary is reused by every slab (the next slab overwrites it while it
+        // is still in L2, so it is never written back to HBM)
+        isize = isize / static_cast<std::size_t>(Kimg) * static_cast<std::size_t>(slab_k);
+        osize = osize / static_cast<std::size_t>(Kimg) * static_cast<std::size_t>(slab_k);
+    }
     if (isize > osize) {
         plan.tmp = std::make_shared<device_buffer>(isize);
     }
-    std::size_t n = plan.passes.size();
-    for (std::size_t i = 0; i < n; ++i) {
-        plan.passes[i].in_sel = i == 0 ? (strided_nd ? 3 : 0) : 2;
-        plan.passes[i].out_sel = i + 1 == n ? (strided_nd ? 4 : 1) : 2;
+    for (auto *pl : {&plan.passes, &plan.tail_passes}) {
+        for (std::size_t i = 0; i < pl->size(); ++i) {
+            (*pl)[i].in_sel = i == 0 ? (strided_nd ? 3 : 0) : 2;
+            (*pl)[i].out_sel = i + 1 == pl->size() ? (strided_nd ? 4 : 1) : 2;
+        }
     }
     if (strided_nd) {
         auto copy_pass = [&](bool gather) {
@@ -1679,8 +1724,10 @@ static void make_plan_impl(bbfft_configuration const &cfg, cudaStream_t stream,
         plan.passes.push_back(copy_pass(false));
     }
     plan.inplace_ok = true;
-    for (auto const &ps : plan.passes) {
-        plan.inplace_ok = plan.inplace_ok && ps.inplace_ok;
+    for (auto *pl : {&plan.passes, &plan.tail_passes}) {
+        for (auto const &ps : *pl) {
+            plan.inplace_ok = plan.inplace_ok && ps.inplace_ok;
+        }
     }
 }
 
@@ -1693,6 +1740,9 @@ static bool pdl_enabled() {
     }();
     return on;
 }
+
+static void run_passes(bbfft_plan_s &plan, std::vector<pass> const &passes, const void *in,
+                       void *out, cudaStream_t stream);
 
 static void execute_impl(bbfft_plan_s &plan, const void *in, void *out, cudaStream_t stream) {
     if (in == out && !plan.inplace_ok) {
@@ -1714,6 +1764,26 @@ static void execute_impl(bbfft_plan_s &plan, const void *in, void *out, cudaStre
         GB_CUDA(cudaSetDevice(plan.device));
         restore.dev = plan.device;
     }
+    if (plan.slab_k > 0) {
+        // L2-resident chaining: every pass over one slab of K, slab after slab; the
+        // temporary aliases the slab's output unless the plan has its own (reused)
+        char const *ib = static_cast<char const *>(in);
+        char *ob = static_cast<char *>(out);
+        for (long long sl = 0; sl < plan.slab_count; ++sl) {
+            run_passes(plan, plan.passes, ib + sl * plan.slab_in_bytes, ob + sl * plan.slab_out_bytes,
+                       stream);
+        }
+        if (!plan.tail_passes.empty()) {
+            run_passes(plan, plan.tail_passes, ib + plan.slab_count * plan.slab_in_bytes,
+                       ob + plan.slab_count * plan.slab_out_bytes, stream);
+        }
+        return;
+    }
+    run_passes(plan, plan.passes, in, out, stream);
+}
+
+static void run_passes(bbfft_plan_s &plan, std::vector<pass> const &passes, const void *in,
+                       void *out, cudaStream_t stream) {
     void *packed_in = plan.packed_in ? plan.packed_in->ptr : nullptr;
     void *packed_out = plan.packed_out ? plan.packed_out->ptr : nullptr;
     void *tmp = plan.tmp ? plan.tmp->ptr : (packed_out ? packed_out : out);
@@ -1731,7 +1801,7 @@ static void execute_impl(bbfft_plan_s &plan, const void *in, void *out, cudaStre
             return tmp;
         }
     };
-    for (auto &pass0 : plan.passes) {
+    for (auto &pass0 : passes) {
         const void *pin = select(pass0.in_sel);
         void *pout = select(pass0.out_sel);
         if (pass0.copy) {
@@ -2503,7 +2573,9 @@ int bbfft_plan_get_info(bbfft_plan_t plan, bbfft_plan_info *info) {
         }
         auto const &ps = *first;
         std::strncpy(info->identifier, ps.identifier.c_str(), sizeof(info->identifier) - 1);
-        info->num_launches = static_cast<uint32_t>(plan->passes.size());
+        info->num_launches = static_cast<uint32_t>(
+            plan->slab_k > 0 ? plan->passes.size() * plan->slab_count + plan->tail_passes.size()
+                             : plan->passes.size());
         info->inplace_supported = plan->inplace_ok;
         info->jit_compiled = plan->jit;
         info->num_stages = static_cast<uint32_t>(ps.p.L);

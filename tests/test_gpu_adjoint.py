@@ -63,24 +63,24 @@ def test_adjoint_identity_fp64(bb, torch_cuda, case):
     assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), 1.0) * 10, (lhs, rhs)
 
 
-def test_spectral_layer_finite_differences_fp64(bb, torch_cuda):
-    """64 random directions, central differences of sum(y^2) in FP64 (exact for a quadratic
-    loss up to rounding), against the autograd gradient through the adjoint kernels."""
-    torch = torch_cuda
+def _spectral_fd(bb, torch, N1, N2, batch, channels, m1, m2, ndir=64):
+    """Central differences of sum(y^2) in FP64 along `ndir` random directions (exact for
+    the polynomial loss up to O(eps^2) and rounding) against the autograd gradient through
+    the adjoint kernels; returns the worst relative error."""
     from bbfft_gb300.autograd import SpectralLayer2d
 
-    layer = SpectralLayer2d(16, 12, 2, 3, 5, 4, prec=bb.F64)
+    layer = SpectralLayer2d(N1, N2, batch, channels, m1, m2, prec=bb.F64)
     gen = torch.Generator(device='cuda')
     gen.manual_seed(7)
-    x = torch.randn(2, 3, 12, 16, generator=gen, device='cuda', dtype=torch.float64,
+    x = torch.randn(batch, channels, N2, N1, generator=gen, device='cuda', dtype=torch.float64,
                     requires_grad=True)
-    w = (torch.randn(3, 4, 5, generator=gen, device='cuda', dtype=torch.float64) * 0.02 +
-         1j * torch.randn(3, 4, 5, generator=gen, device='cuda', dtype=torch.float64) * 0.02)
+    w = (torch.randn(channels, m2, m1, generator=gen, device='cuda', dtype=torch.float64) * 0.02 +
+         1j * torch.randn(channels, m2, m1, generator=gen, device='cuda', dtype=torch.float64) * 0.02)
     w = w.requires_grad_(True)
     loss = (layer(x, w) ** 2).sum()
     gx, gw = torch.autograd.grad(loss, (x, w))
     worst = 0.0
-    for i in range(64):
+    for i in range(ndir):
         vx = torch.randn(x.shape, generator=gen, device='cuda', dtype=torch.float64)
         # directions on the scale of each variable (weights ~ 0.02); the loss is quartic in
         # the step, so the central difference carries a relative error ~ (eps |v| / |w|)^2
@@ -94,6 +94,19 @@ def test_spectral_layer_finite_differences_fp64(bb, torch_cuda):
         an = float((gx * vx).sum() + (torch.view_as_real(gw) * torch.view_as_real(vw)).sum())
         rel = abs(fd - an) / max(abs(an), 1e-30)
         worst = max(worst, rel)
+    return worst
+
+
+def test_spectral_layer_finite_differences_fp64(bb, torch_cuda):
+    """A small layer (16 x 12, K = 2 x 3, 5 x 4 modes): 64 directions, FP64, 1e-6."""
+    assert _spectral_fd(bb, torch_cuda, 16, 12, 2, 3, 5, 4) <= 1e-6
+
+
+def test_spectral_layer_finite_differences_fp64_benchmark_shape(bb, torch_cuda):
+    """The benchmark's layer: 2d r2c / c2r over 128 x 128, K = 64 batch x 32 channels,
+    lowest 32 x 32 modes, 64 random directions in FP64, relative error <= 1e-6."""
+    worst = _spectral_fd(bb, torch_cuda, 128, 128, 64, 32, 32, 32)
+    print('worst FD relative error', worst)
     assert worst <= 1e-6, worst
 
 

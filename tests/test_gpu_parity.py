@@ -455,3 +455,51 @@ def test_transpose_fft_transpose_equals_double_batched(bb, torch_cuda):
     torch.cuda.synchronize()
     y2 = xt.permute(0, 2, 1)
     assert float(torch.linalg.vector_norm(y - y2) / torch.linalg.vector_norm(y2)) <= 1e-6
+
+
+# ------------------------------------------------- nd plans run slab by slab through L2
+
+# intermediates larger than a quarter of the L2 cache: the plan runs its passes slab by slab
+# along K (a full slab and a shorter last one for these K)
+ND_SLABS = [
+    (2, [1, 128, 128, 700], 1, False), (2, [1, 128, 128, 700], 2, False),
+    (2, [1, 128, 128, 700], 1, True), (3, [1, 64, 64, 64, 20], 0, False),
+    (2, [2, 96, 80, 900], 0, False),
+]
+
+
+@pytest.mark.parametrize('case', ND_SLABS, ids=[str(c) for c in ND_SLABS])
+def test_nd_plans_in_l2_slabs(bb, po, torch_cuda, case):
+    """nd float plans whose intermediate tensor exceeds a quarter of L2 (so they run slab by
+    slab along K): images at the start, inside and at the end of the tensor, around slab
+    boundaries, against the oracle in FP64."""
+    torch = torch_cuda
+    dim, shape, type, inplace = case
+    K = shape[-1]
+    rng = np.random.default_rng(sum(shape) + type)
+    d = bb.BACKWARD if type == 2 else bb.FORWARD
+    cfg = bb.configuration(dim, shape, precision=bb.F32, type=type, direction=d, inplace=inplace)
+    plan = bb.Plan(cfg, stream=torch.cuda.current_stream().cuda_stream)
+    info = plan.info()
+    assert info.num_launches > dim, 'expected a slabbed plan'
+    ist = list(cfg.istride)[:dim + 2]
+    ost = list(cfg.ostride)[:dim + 2]
+    in_per_k, out_per_k = ist[dim + 1], ost[dim + 1]
+    cplx_in, cplx_out = type != 1, type != 2
+    n_in = in_per_k * K
+    if cplx_in:
+        x = (rng.standard_normal(n_in) + 1j * rng.standard_normal(n_in)).astype(np.complex64)
+    else:
+        x = rng.standard_normal(n_in).astype(np.float32)
+    out_dt = np.complex64 if cplx_out else np.float32
+    out = run(bb, torch, cfg, x, out_per_k * K, out_dt, inplace=inplace, plan=plan)
+    picks = sorted(set([0, 1, K // 3, K // 2 - 1, K // 2, K - 2, K - 1]))
+    sub_shape = list(shape[:-1]) + [len(picks)]
+    xs = np.concatenate([x[k * in_per_k:(k + 1) * in_per_k] for k in picks])
+    cfg_s = bb.configuration(dim, sub_shape, precision=bb.F32, type=type, direction=d, inplace=inplace)
+    ref = po.oracle_fft(dim, sub_shape, type, d, xs.astype(np.complex128 if cplx_in else np.float64),
+                        istride=ist[:dim + 1] + [in_per_k], ostride=ost[:dim + 1] + [out_per_k],
+                        inplace=inplace, prec=8)
+    got = np.concatenate([out[k * out_per_k:(k + 1) * out_per_k] for k in picks])
+    e = rel_l2(got, ref)
+    assert e <= TOL[4], e
