@@ -760,8 +760,12 @@ def leg_c2c_3d(bb, torch, stream, hbm_peak, steps, warmup):
 
     ms = event_time(torch, stream, both, max(steps, 3))
     bytes_ = 2 * 3 * 2 * n * 8  # 2 transforms x 3 passes x (read + write)
+    once = 2 * 2 * n * 8        # 2 transforms x one read + one write of the tensor
     return {'ms_fwd_bwd': round(ms, 3), 'gbs_all_passes': round(bytes_ / ms / 1e6, 1),
-            'frac_of_hbm': round(bytes_ / ms / 1e6 / hbm_peak, 3)}
+            'gbs_one_read_one_write': round(once / ms / 1e6, 1),
+            'frac_of_hbm': round(once / ms / 1e6 / hbm_peak, 3),
+            'note': 'the passes run slab by slab along K through L2, so HBM sees about one '
+                    'read and one write per transform; frac_of_hbm uses those bytes'}
 
 
 # MMAs (mma.sync m16n8k8 TF32, 2048 flops each with the padding) per transform of the

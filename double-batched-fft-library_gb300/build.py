@@ -7,19 +7,22 @@ text (engine_src.inc) so that plans with user callbacks can be compiled by NVRTC
 run time.  Outputs are rebuilt only when a source is newer than the library.
 """
 import concurrent.futures as cf
+import hashlib
 import os
 import shutil
 import subprocess
 import sys
+import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, 'csrc')
 REPO = os.path.dirname(HERE)
 INCLUDE = os.path.join(REPO, 'include')
 OUTDIR = os.path.join(HERE, 'bbfft_gb300', '_lib')
-# object files and generated sources (BBFFT_GB300_BUILD_DIR moves them, e.g. out of a tree
-# that is copied elsewhere)
-BUILD = os.environ.get('BBFFT_GB300_BUILD_DIR') or os.path.join(HERE, '_build')
+# object files and generated sources: outside the source tree (hundreds of MB that a copy of
+# the tree should not carry), one directory per checkout; BBFFT_GB300_BUILD_DIR overrides
+BUILD = os.environ.get('BBFFT_GB300_BUILD_DIR') or os.path.join(
+    tempfile.gettempdir(), 'bbfft_gb300_build_' + hashlib.sha1(HERE.encode()).hexdigest()[:10])
 LIB = os.path.join(OUTDIR, 'libbbfft_gb300.so')
 # throughput probes for the benchmark's roofline denominators (not part of the library)
 PROBES_SRC = os.path.join(CSRC, 'peak_probes.cu')
