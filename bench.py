@@ -136,39 +136,61 @@ def dist_env():
 # CPU baseline (oracle port)
 
 
-def cpu_baseline(prec=4, budget_s=12.0, threads=None):
-    """Time the oracle's r2c+c2r over a K-subset of every N of the sweep on all host cores."""
-    from oracle import pyoracle as po
+def cpu_sample_k(N, threads):
+    """Slices of the CPU sample for length N: 2^20 / N of them (about 64 MB per pass, the
+    same bytes for every N), at least two per host thread, at most the full tensor."""
+    return max(2 * threads, min(k_for(N, 4), (1 << 20) // N))
 
-    threads = threads or os.cpu_count() or 1
-    rng = np.random.default_rng(0)
-    rdt = np.float32 if prec == 4 else np.float64
-    cdt = np.complex64 if prec == 4 else np.complex128
-    total_bytes, total_t = 0, 0.0
-    per_n_budget = budget_s / len(SWEEP_N)
-    for N in SWEEP_N:
-        Kfull = k_for(N, prec)
-        K = max(2 * threads, min(Kfull, 4096 * 64 // N))
-        x = rng.standard_normal(M_BATCH * N * K).astype(rdt)
-        X = np.zeros(M_BATCH * (N // 2 + 1) * K, dtype=cdt)
-        y = np.zeros(M_BATCH * N * K, dtype=rdt)
-        reps, t_n = 0, 0.0
-        while t_n < per_n_budget or reps == 0:
-            t0 = time.perf_counter()
+
+class CpuSample:
+    """The oracle's r2c + c2r (the C restatement of the reference's algorithm) on all host
+    cores over a fixed K-subset of every N of the sweep.  The buffers are allocated and
+    touched once (an untimed sweep), so every timed sweep does the same work."""
+
+    def __init__(self, prec=4, threads=None):
+        from oracle import pyoracle as po
+
+        self.po = po
+        self.prec = prec
+        self.threads = threads or os.cpu_count() or 1
+        rng = np.random.default_rng(0)
+        rdt = np.float32 if prec == 4 else np.float64
+        cdt = np.complex64 if prec == 4 else np.complex128
+        self.cases = []
+        for N in SWEEP_N:
+            K = cpu_sample_k(N, self.threads)
+            x = rng.standard_normal(M_BATCH * N * K).astype(rdt)
+            X = np.zeros(M_BATCH * (N // 2 + 1) * K, dtype=cdt)
+            y = np.zeros(M_BATCH * N * K, dtype=rdt)
+            self.cases.append((N, K, x, X, y))
+        self.bytes = sum(2 * pass_bytes(N, K, prec) for (N, K, _, _, _) in self.cases)
+        self.sweep()  # first touch of every page
+
+    def sweep(self):
+        """One timed pass over the sample; returns seconds."""
+        po, prec, th = self.po, self.prec, self.threads
+        t0 = time.perf_counter()
+        for N, K, x, X, y in self.cases:
             po.fft1d(po.R2C, po.FORWARD, M_BATCH, N, K, x, M_BATCH, M_BATCH * N, X, M_BATCH,
-                     M_BATCH * (N // 2 + 1), prec, threads)
+                     M_BATCH * (N // 2 + 1), prec, th)
             po.fft1d(po.C2R, po.BACKWARD, M_BATCH, N, K, X, M_BATCH, M_BATCH * (N // 2 + 1), y,
-                     M_BATCH, M_BATCH * N, prec, threads)
-            t_n += time.perf_counter() - t0
-            reps += 1
-        total_bytes += 2 * pass_bytes(N, K, prec) * reps
-        total_t += t_n
-    return {'value': total_bytes / total_t / 1e9, 'unit': 'GB/s', 'cores': threads,
-            'kind': 'port',
-            'sample': 'oracle r2c+c2r, M=8, every N of the sweep, K-subset of %d..%d slices per N, '
-                      '%.0f s total' % (min(max(2 * threads, 4096 * 64 // n) for n in SWEEP_N),
-                                        max(max(2 * threads, 4096 * 64 // n) for n in SWEEP_N),
-                                        total_t)}
+                     M_BATCH, M_BATCH * N, prec, th)
+        return time.perf_counter() - t0
+
+    def describe(self, secs):
+        ks = [K for (_, K, _, _, _) in self.cases]
+        return ('oracle r2c+c2r, M=8, every N of the sweep, K-subset of %d..%d slices per N '
+                '(2^20 / N, %.2f GB per sweep), %.1f s timed' % (min(ks), max(ks), self.bytes / 1e9,
+                                                                 secs))
+
+
+def cpu_baseline(prec=4, sweeps=3, threads=None):
+    """GB/s of the CPU sample over `sweeps` timed sweeps (the reference arm times the same
+    sample, one sweep per step)."""
+    smp = CpuSample(prec, threads)
+    t = sum(smp.sweep() for _ in range(sweeps))
+    return {'value': smp.bytes * sweeps / t / 1e9, 'unit': 'GB/s', 'cores': smp.threads,
+            'kind': 'port', 'sample': smp.describe(t)}
 
 
 def run_reference(args):
@@ -176,28 +198,26 @@ def run_reference(args):
     if rank != 0:
         return
     prec = 4
-    res = None
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        cpu_baseline(prec, budget_s=2.0)
-    vals = []
-    t0 = time.perf_counter()
+    smp = CpuSample(prec)
+    for _ in range(max(0, args.warmup)):
+        smp.sweep()
+    t = 0.0
     for _ in range(args.steps):
-        res = cpu_baseline(prec, budget_s=max(3.0, 60.0 / max(1, args.steps)))
-        vals.append(res['value'])
-    elapsed = time.perf_counter() - t0
-    value = float(np.median(vals))
+        t += smp.sweep()
+    value = smp.bytes * args.steps / t / 1e9
     line = {
         'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': 'GB/s', 'n_gpus': ws,
         'steps': args.steps, 'warmup': args.warmup,
-        'ms_per_step': elapsed / args.steps * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+        'ms_per_step': t / args.steps * 1e3, 'higher_is_better': True, 'scaling': 'weak',
         'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic: iid N(0,1) reals, seeded',
         'config': {'workload': 'r2c+c2r round trip, M=8, 1 GiB real input per N, f32, '
                                'N in ' + str(SWEEP_N) + ' (K-subset on the CPU)'},
-        'cpu_baseline': {'value': value, 'unit': 'GB/s', 'cores': res['cores'], 'kind': 'port',
-                         'sample': res['sample']},
+        'cpu_baseline': {'value': value, 'unit': 'GB/s', 'cores': smp.threads, 'kind': 'port',
+                         'sample': smp.describe(t)},
         'e2e': {'value': value, 'unit': 'GB/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
         'note': 'reference CPU path = C restatement of the reference kernels (oracle/); the '
-                'reference library itself needs an OpenCL/SYCL/Level Zero runtime',
+                'reference library itself needs an OpenCL/SYCL/Level Zero runtime; the GPU '
+                'line\'s cpu_baseline times the same sample',
     }
     print(json.dumps(line), flush=True)
 
@@ -365,7 +385,7 @@ def run_ours(args):
         'legs': legs,
     }
     if rank == 0 and not args.no_cpu:
-        line['cpu_baseline'] = cpu_baseline(prec, budget_s=args.cpu_seconds)
+        line['cpu_baseline'] = cpu_baseline(prec, sweeps=args.cpu_sweeps)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -976,7 +996,7 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--no-cpu', action='store_true')
-    ap.add_argument('--cpu-seconds', type=float, default=15.0)
+    ap.add_argument('--cpu-sweeps', type=int, default=3, help='timed sweeps of the CPU sample')
     ap.add_argument('--no-legs', action='store_true', help='headline workload only')
     ap.add_argument('--legs', default='all',
                     help='comma-separated secondary legs to run (default: all): ' + ','.join(LEGS))
