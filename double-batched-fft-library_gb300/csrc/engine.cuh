@@ -42,16 +42,6 @@
 
 namespace gbfft {
 
-// Programmatic dependent launch.  Plan kernels may be launched while the previous kernel
-// of the stream is still running (cudaLaunchAttributeProgrammaticStreamSerialization):
-// each lets the next launch be scheduled early, then waits until the previous kernel has
-// finished and its memory is visible before it touches global memory.  Without the launch
-// attribute both instructions are no-ops.
-__device__ __forceinline__ void pdl_prologue() {
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-}
-
 // Default memory access policy: plain loads and stores at tensor + base + off.  The
 // JIT path generates a policy with the same interface that calls user callbacks with
 // the element offset base + off (reference callback_accessor,

@@ -211,6 +211,13 @@ def ragged_entries():
     return out
 
 
+def tile_min_blocks(rad):
+    """Resident 256-thread CTAs the register budget of a tile kernel is sized for: 3 (80
+    registers) with a tensor-core prime stage, whose tiles are otherwise limited by the
+    latency of 2 CTAs per SM at 128 registers; 2 for the others."""
+    return 3 if any(r in BIG_PRIMES for r in rad) else 2
+
+
 def largest_prime_factor(n):
     return max(prime_factors(n)) if n > 1 else 1
 
@@ -248,8 +255,7 @@ def cover_units(outdir):
         for i in idx:
             prec, kind, nc, T, rad, V = ents[i]
             targs = 'float, %d, %d, %d, %d, %s' % (kind, nc, T, V, ', '.join(map(str, rad)))
-            src += ['__global__ void __launch_bounds__(256, 2) cover_ct_%d(const __grid_constant__ fft_params p) {' % i,
-                    '    pdl_prologue();',
+            src += ['__global__ void __launch_bounds__(256, %d) cover_ct_%d(const __grid_constant__ fft_params p) {' % (tile_min_blocks(rad), i),
                     '    fft_tile_ct_ragged<%s>(p, blockIdx.x);' % targs, '}', '']
         src += ['const void *cover_ct_kernel_%d(int i) {' % g, '    switch (i) {']
         for i in idx:
@@ -316,14 +322,13 @@ def ragged_units(outdir):
             src += ['__device__ __noinline__ void ragged_ct_%d(const fft_params &p, long long tile) {' % i,
                     '    fft_tile_ct_ragged<%s>(p, tile);' % targs,
                     '}', '',
-                    '__global__ void __launch_bounds__(256, 2) ragged_class_ct_%d(const ragged_item_dev *__restrict__ items,' % i,
+                    '__global__ void __launch_bounds__(256, %d) ragged_class_ct_%d(const ragged_item_dev *__restrict__ items,' % (tile_min_blocks(rad), i),
                     '                                                        const int2 *__restrict__ units) {',
                     '    __shared__ __align__(16) fft_params s_p;',
                     '    const int2 un = stage_unit_params(items, units, s_p);',
                     '    fft_tile_ct_ragged<%s>(s_p, un.y);' % targs,
                     '}', '',
-                    '__global__ void __launch_bounds__(256, 2) plan_ct_%d(const __grid_constant__ fft_params p) {' % i,
-                    '    pdl_prologue();',
+                    '__global__ void __launch_bounds__(256, %d) plan_ct_%d(const __grid_constant__ fft_params p) {' % (tile_min_blocks(rad), i),
                     '    fft_tile_ct_ragged<%s>(p, blockIdx.x);' % targs,
                     '}', '']
         for kname in ('ragged_class_ct', 'plan_ct'):
@@ -399,7 +404,6 @@ def main(outdir):
                '#include "engine_ct.cuh"', '#include "kernels.hpp"', '', 'namespace gbfft {', '',
                'template <class R, int Kind, int NC, int TT, int V, int MINB, int... Ps>',
                '__global__ void __launch_bounds__(256, MINB % 10) fft_kernel_ct(const __grid_constant__ fft_params p) {',
-               '    pdl_prologue();',
                '    fft_tile_ct<R, Kind, NC, TT, V, (MINB >= 10), Ps...>(p);', '}', '',
                'extern const ct_entry %s[] = {' % name]
         for nc, T, rad, V, minb in lst:

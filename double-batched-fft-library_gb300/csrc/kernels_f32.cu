@@ -7,7 +7,6 @@ namespace gbfft {
 
 template <class R, int Kind>
 __global__ void __launch_bounds__(512) fft_kernel(const __grid_constant__ fft_params p) {
-    pdl_prologue();
     fft_tile<R, Kind, default_io>(p);
 }
 

@@ -1651,7 +1651,11 @@ static void make_plan_impl(bbfft_configuration const &cfg, cudaStream_t stream,
     std::size_t const inter_per_k = std::max(isize, osize) / static_cast<std::size_t>(Kimg);
     int l2 = 0;
     GB_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, plan.device));
-    std::size_t const budget = static_cast<std::size_t>(l2) / 4;
+    std::size_t budget = static_cast<std::size_t>(l2) / 4;
+    // BBFFT_GB300_ND_SLAB_BYTES overrides the intermediate bytes per slab (0: no slabs)
+    if (const char *e = std::getenv("BBFFT_GB300_ND_SLAB_BYTES")) {
+        budget = static_cast<std::size_t>(std::strtoull(e, nullptr, 10));
+    }
     long long slab_k = 0;
     if (!has_cb && !strided_nd && budget > 0 && inter_per_k * Kimg > budget) {
         slab_k = std::max<long long>(1, static_cast<long long>(budget / inter_per_k));
@@ -1729,16 +1733,6 @@ static void make_plan_impl(bbfft_configuration const &cfg, cudaStream_t stream,
             plan.inplace_ok = plan.inplace_ok && ps.inplace_ok;
         }
     }
-}
-
-// Programmatic dependent launch of the plan kernels (all of them call pdl_prologue);
-// BBFFT_GB300_PDL=0 turns it off.
-static bool pdl_enabled() {
-    static const bool on = [] {
-        const char *e = std::getenv("BBFFT_GB300_PDL");
-        return !(e && std::strcmp(e, "0") == 0);
-    }();
-    return on;
 }
 
 static void run_passes(bbfft_plan_s &plan, std::vector<pass> const &passes, const void *in,
@@ -1835,24 +1829,7 @@ static void run_passes(bbfft_plan_s &plan, std::vector<pass> const &passes, cons
             p.flags &= ~flag_vec_out;
         }
         void *args[] = {&p};
-        cudaError_t e;
-        if (!ps.mod && pdl_enabled()) {
-            // programmatic dependent launch: the kernel waits for the previous kernel of the
-            // stream itself (pdl_prologue), so its launch may overlap that kernel's tail
-            cudaLaunchConfig_t lc = {};
-            lc.gridDim = dim3(ps.grid);
-            lc.blockDim = dim3(ps.block);
-            lc.dynamicSmemBytes = ps.smem;
-            lc.stream = stream;
-            cudaLaunchAttribute attr[1];
-            attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-            attr[0].val.programmaticStreamSerializationAllowed = 1;
-            lc.attrs = attr;
-            lc.numAttrs = 1;
-            e = cudaLaunchKernelExC(&lc, ps.func, args);
-        } else {
-            e = cudaLaunchKernel(ps.func, dim3(ps.grid), dim3(ps.block), args, ps.smem, stream);
-        }
+        cudaError_t e = cudaLaunchKernel(ps.func, dim3(ps.grid), dim3(ps.block), args, ps.smem, stream);
         if (e != cudaSuccess) {
             throw status_error(BBFFT_CUDA_ERROR,
                                std::string("kernel launch failed: ") + cudaGetErrorString(e));

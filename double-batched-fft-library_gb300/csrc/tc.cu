@@ -287,7 +287,6 @@ __device__ __forceinline__ void load_tile(const float2 *x, float2 *buf, long lon
 // radix-16 / 32 stages on the tensor cores, the radix-2 stage on the CUDA cores.
 template <int NC> __global__ void __launch_bounds__(kThreads, 3) fft_tc32_kernel(const __grid_constant__ fft_params p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    pdl_prologue();
     constexpr int tiles = kElems / NC;
     float2 *buf0 = reinterpret_cast<float2 *>(smem_raw);
     float2 *buf1 = buf0 + kBufElems;
@@ -316,7 +315,6 @@ template <int NC> __global__ void __launch_bounds__(kThreads, 3) fft_tc32_kernel
 // c2c float, M = 1, packed: tiles of kElems / NC transforms per CTA.
 template <int PIECES, int NC> __global__ void __launch_bounds__(kThreads, 3) fft_tc_kernel(const __grid_constant__ fft_params p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    pdl_prologue();
     constexpr int tiles = kElems / NC;
     float2 *buf0 = reinterpret_cast<float2 *>(smem_raw);
     float2 *buf1 = buf0 + kBufElems;
