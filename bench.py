@@ -783,9 +783,9 @@ def leg_c2c_3d(bb, torch, stream, hbm_peak, steps, warmup):
     once = 2 * 2 * n * 8        # 2 transforms x one read + one write of the tensor
     return {'ms_fwd_bwd': round(ms, 3), 'gbs_all_passes': round(bytes_ / ms / 1e6, 1),
             'gbs_one_read_one_write': round(once / ms / 1e6, 1),
-            'frac_of_hbm': round(once / ms / 1e6 / hbm_peak, 3),
-            'note': 'the passes run slab by slab along K through L2, so HBM sees about one '
-                    'read and one write per transform; frac_of_hbm uses those bytes'}
+            'frac_of_hbm': round(bytes_ / ms / 1e6 / hbm_peak, 3),
+            'note': 'gbs_all_passes and frac_of_hbm count one read + one write per pass (three '
+                    'passes per transform); gbs_one_read_one_write counts one per transform'}
 
 
 # MMAs (mma.sync m16n8k8 TF32, 2048 flops each with the padding) per transform of the

@@ -1642,17 +1642,16 @@ static void make_plan_impl(bbfft_configuration const &cfg, cudaStream_t stream,
     std::size_t isize = ist[dim + 1] * cfg.shape[dim + 1] * (in_real ? real_b : cplx_b);
     std::size_t osize = ost[dim + 1] * cfg.shape[dim + 1] * (out_real ? real_b : cplx_b);
     // L2-resident chaining (no counterpart in the reference, which runs each pass over the
-    // whole tensor, nd_fft.hpp:140-152): when the intermediate tensor is larger than a
-    // quarter of the L2 cache, the passes run slab by slab along K, so the intermediate
-    // written by one pass is still in L2 when the next pass reads it and HBM sees about one
-    // read of the input and one write of the output.  Not with callbacks (their offsets are
-    // relative to the whole tensor) or custom layouts (packed copies).
+    // whole tensor, nd_fft.hpp:140-152): with BBFFT_GB300_ND_SLAB_BYTES = B > 0 and an
+    // intermediate tensor larger than B, the passes run slab by slab along K (slabs of at
+    // most B intermediate bytes), so the intermediate written by one pass can still be in
+    // L2 when the next pass reads it.  Off by default: on GB300 the 2d 128 x 128 and 3d 64^3
+    // benchmark plans ran slower in slabs of L2/4 or 64 MB (more, shorter launches) than
+    // over the whole tensor.  Not with callbacks (their offsets are relative to the whole
+    // tensor) or custom layouts (packed copies).
     long long const Kimg = static_cast<long long>(cfg.shape[dim + 1]);
     std::size_t const inter_per_k = std::max(isize, osize) / static_cast<std::size_t>(Kimg);
-    int l2 = 0;
-    GB_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, plan.device));
-    std::size_t budget = static_cast<std::size_t>(l2) / 4;
-    // BBFFT_GB300_ND_SLAB_BYTES overrides the intermediate bytes per slab (0: no slabs)
+    std::size_t budget = 0;
     if (const char *e = std::getenv("BBFFT_GB300_ND_SLAB_BYTES")) {
         budget = static_cast<std::size_t>(std::strtoull(e, nullptr, 10));
     }

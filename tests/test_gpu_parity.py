@@ -459,8 +459,8 @@ def test_transpose_fft_transpose_equals_double_batched(bb, torch_cuda):
 
 # ------------------------------------------------- nd plans run slab by slab through L2
 
-# intermediates larger than a quarter of the L2 cache: the plan runs its passes slab by slab
-# along K (a full slab and a shorter last one for these K)
+# intermediates larger than 32 MB: with BBFFT_GB300_ND_SLAB_BYTES = 32 MB the plan runs its
+# passes slab by slab along K (full slabs and a shorter last one for these K)
 ND_SLABS = [
     (2, [1, 128, 128, 700], 1, False), (2, [1, 128, 128, 700], 2, False),
     (2, [1, 128, 128, 700], 1, True), (3, [1, 64, 64, 64, 20], 0, False),
@@ -469,17 +469,19 @@ ND_SLABS = [
 
 
 @pytest.mark.parametrize('case', ND_SLABS, ids=[str(c) for c in ND_SLABS])
-def test_nd_plans_in_l2_slabs(bb, po, torch_cuda, case):
-    """nd float plans whose intermediate tensor exceeds a quarter of L2 (so they run slab by
-    slab along K): images at the start, inside and at the end of the tensor, around slab
-    boundaries, against the oracle in FP64."""
+def test_nd_plans_in_l2_slabs(bb, po, torch_cuda, monkeypatch, case):
+    """nd float plans run slab by slab along K (BBFFT_GB300_ND_SLAB_BYTES = 32 MB, smaller
+    than their intermediate tensors): images at the start, inside and at the end of the
+    tensor, around slab boundaries, against the oracle in FP64."""
     torch = torch_cuda
     dim, shape, type, inplace = case
     K = shape[-1]
     rng = np.random.default_rng(sum(shape) + type)
     d = bb.BACKWARD if type == 2 else bb.FORWARD
     cfg = bb.configuration(dim, shape, precision=bb.F32, type=type, direction=d, inplace=inplace)
+    monkeypatch.setenv('BBFFT_GB300_ND_SLAB_BYTES', str(32 << 20))
     plan = bb.Plan(cfg, stream=torch.cuda.current_stream().cuda_stream)
+    monkeypatch.delenv('BBFFT_GB300_ND_SLAB_BYTES')
     info = plan.info()
     assert info.num_launches > dim, 'expected a slabbed plan'
     ist = list(cfg.istride)[:dim + 2]
