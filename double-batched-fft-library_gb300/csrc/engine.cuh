@@ -285,11 +285,15 @@ __device__ __forceinline__ void run_stage_prime_tc(const transform_ctx<R, Kind, 
     const float2 *tw = static_cast<const float2 *>(p.tw);
     float2 *sm = c.sm;
     const int pshift = c.pshift, padd = c.padd, bufe = c.bufe;
+    // butterflies in groups of 8: the same butterfly of 8 neighbouring transforms when
+    // Mb >= 8 (adjacent in shared memory), else 8 butterflies of one transform
+    const int ntr = mb * p.Kb;
+    const bool mfast = mb >= 8;
     for (int grp = threadIdx.x >> 5; grp < ngrp; grp += nwarps) {
         const int q = grp * 8 + (lane >> 2);
         const bool valid = q < nbf;
-        const int tr = valid ? q / nb : 0;
-        const int b = valid ? q - tr * nb : 0;
+        const int tr = !valid ? 0 : mfast ? q % ntr : q / nb;
+        const int b = !valid ? 0 : mfast ? q / ntr : q - tr * nb;
         const int base = (tr / mb) * p.Nc * mb + (tr % mb);
         const int kk = b % Ns;
         const int o = b + (b / Ns) * Ns * (P - 1);

@@ -349,11 +349,16 @@ __device__ __forceinline__ void ct_stage_prime_tc(const Ctx &c) {
     const float2 *tw = static_cast<const float2 *>(p.tw);
     float2 *sm = c.sm;
     const int pshift = c.pshift, padd = c.padd;
+    // butterflies in groups of 8: with 8 or more transforms along M the group's butterflies
+    // are the same butterfly of 8 neighbouring transforms (adjacent in shared memory), else
+    // 8 butterflies of one transform (adjacent when Mb = 1)
+    const int ntr = mb * p.Kb;
+    const bool mfast = mb >= 8;
     for (int grp = threadIdx.x >> 5; grp < ngrp; grp += nwarps) {
         const int q = grp * 8 + (lane >> 2);
         const bool valid = q < nbf;
-        const int tr = valid ? q / nb : 0;
-        const int b = valid ? q - tr * nb : 0;
+        const int tr = !valid ? 0 : mfast ? q % ntr : q / nb;
+        const int b = !valid ? 0 : mfast ? q / ntr : q - tr * nb;
         const int base = (tr / mb) * NC * mb + (tr % mb) + b * mb;
         auto at = [&](int n) {
             const int i = base + n * (nb * mb);
