@@ -365,6 +365,38 @@ def test_prime_factor_lengths(bb, po, torch_cuda, type):
     print('worst rel-L2', worst)
 
 
+# every length up to 512 with a prime factor above 61 (tensor-core stage with coefficients
+# from the w_P table, runtime-size engine)
+BIG_PRIME_N = [n for n in range(67, 513) if _largest_prime_factor(n) > 61]
+
+
+@pytest.mark.parametrize('type', [0, 1, 2])
+def test_big_prime_factor_lengths(bb, po, torch_cuda, type):
+    """Float plans of every N <= 512 whose largest prime factor is above 61, random double
+    batching, against the oracle in FP64 within the float tolerance."""
+    torch = torch_cuda
+    rng = np.random.default_rng(21 + type)
+    worst = 0.0
+    for N in BIG_PRIME_N:
+        M = int(rng.choice([1, 2, 8, 16]))
+        K = int(rng.integers(1, 12))
+        d = bb.BACKWARD if type == 2 else (bb.FORWARD if type == 1 else
+                                           int(rng.choice([bb.FORWARD, bb.BACKWARD])))
+        cfg = bb.configuration(1, [M, N, K], precision=bb.F32, type=type, direction=d)
+        nin = N // 2 + 1 if type == 2 else N
+        nout = N // 2 + 1 if type == 1 else N
+        if type == 1:
+            x = rng.standard_normal(M * nin * K).astype(np.float32)
+        else:
+            x = (rng.standard_normal(M * nin * K) + 1j * rng.standard_normal(M * nin * K)).astype(np.complex64)
+        out = run(bb, torch, cfg, x, M * nout * K, np.float32 if type == 2 else np.complex64)
+        ref = po.oracle_fft(1, [M, N, K], type, d, x.astype(np.complex128 if type != 1 else np.float64), prec=8)
+        e = rel_l2(out, ref)
+        worst = max(worst, e)
+        assert e <= TOL[4], (N, M, K, d, e)
+    print('worst rel-L2', worst)
+
+
 @pytest.mark.parametrize('type,N,M', [(1, 160, 8), (2, 160, 8), (0, 64, 1), (2, 384, 8), (1, 96, 8)])
 def test_tuned_variants_agree(bb, po, torch_cuda, type, N, M):
     """Every blocking the autotuner may pick (V, Mb, Kb, 2 or 3 resident CTAs) gives the
