@@ -309,150 +309,6 @@ __device__ __forceinline__ void run_stage_prime_tc(const transform_ctx<R, Kind, 
     }
 }
 
-// Float prime radix above 61 on the tensor cores: the same products as
-// ptc::butterflies8, with the coefficient fragments formed on the fly from the w_P table
-// in shared memory (wtab[q] = w_P^{-q} = (cos, -sin)(2 pi q / P), q < P; the index j k mod P
-// advances by 8 k mod P per k-step) and split into two TF32 pieces, and the output pairs
-// taken NTC n-tiles at a time so that the accumulators fit in registers (the input pairs
-// are loaded again for every group of n-tiles).  Shared source buffer to shared destination
-// buffer, stage twiddles applied as the inputs are loaded.
-template <class R, int Kind, class IO>
-__device__ __forceinline__ void run_stage_bigprime_tc(const transform_ctx<R, Kind, IO> &c, int P,
-                                                      int Ns, int src_buf, int dst_buf,
-                                                      const float2 *wtab) {
-    constexpr int NTC = 4;
-    const fft_params &p = c.p;
-    const int nb = p.Nc / P;
-    const int mb = p.Mb;
-    const int ntr = mb * p.Kb;
-    const int nbf = ntr * nb;
-    const int ngrp = (nbf + 7) / 8;
-    const int lane = threadIdx.x & 31;
-    const int g = lane >> 2, t = lane & 3;
-    const int nwarps = blockDim.x >> 5;
-    const int twstride = p.Nt / (Ns * P);
-    const int H = (P - 1) / 2;
-    const int KS = (H + 7) / 8;
-    const float2 *tw = static_cast<const float2 *>(p.tw);
-    float2 *sm = c.sm;
-    const int pshift = c.pshift, padd = c.padd, bufe = c.bufe;
-    const bool mfast = mb >= 8;
-    for (int grp = threadIdx.x >> 5; grp < ngrp; grp += nwarps) {
-        const int q = grp * 8 + g;
-        const bool valid = q < nbf;
-        const int tr = !valid ? 0 : mfast ? q % ntr : q / nb;
-        const int b = !valid ? 0 : mfast ? q / ntr : q - tr * nb;
-        const int base = (tr / mb) * p.Nc * mb + (tr % mb);
-        const int twb = (b % Ns) * twstride;
-        const int o = b + (b / Ns) * Ns * (P - 1);
-        auto in = [&](int r) {
-            const int i = base + (b + r * nb) * mb;
-            return sm + src_buf * bufe + i + (i >> pshift) * padd;
-        };
-        auto out = [&](int k) {
-            const int i = base + (o + k * Ns) * mb;
-            return sm + dst_buf * bufe + i + (i >> pshift) * padd;
-        };
-        const float2 x0 = valid ? *in(0) : make_float2(0.f, 0.f);
-        float sre = 0.f, sim = 0.f;
-        for (int nt0 = 0; nt0 < KS; nt0 += NTC) {
-            float u[NTC][4], w[NTC][4];
-            int qa[NTC], qb[NTC], step[NTC];
-#pragma unroll
-            for (int n = 0; n < NTC; ++n) {
-                const int k = 8 * (nt0 + n) + g + 1;
-                qa[n] = ((t + 1) * k) % P; // j0 k mod P, j0 = t + 1 at k-step 0
-                qb[n] = ((t + 5) * k) % P; // j1 = j0 + 4
-                step[n] = (8 * k) % P;
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    u[n][e] = 0.f;
-                    w[n][e] = 0.f;
-                }
-            }
-            for (int ks = 0; ks < KS; ++ks) {
-                float sv[4], dv[4];
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int jj = 8 * ks + t + 1 + 4 * h;
-                    float2 a = make_float2(0.f, 0.f), bv = make_float2(0.f, 0.f);
-                    if (valid && jj <= H) {
-                        a = *in(jj);
-                        bv = *in(P - jj);
-                        if (twb) {
-                            const float2 wa = __ldg(tw + jj * twb);
-                            const float2 wb = __ldg(tw + (P - jj) * twb);
-                            a = make_float2(a.x * wa.x - a.y * wa.y, a.x * wa.y + a.y * wa.x);
-                            bv = make_float2(bv.x * wb.x - bv.y * wb.y, bv.x * wb.y + bv.y * wb.x);
-                        }
-                    }
-                    sv[2 * h] = a.x + bv.x;
-                    sv[2 * h + 1] = a.y + bv.y;
-                    dv[2 * h] = a.x - bv.x;
-                    dv[2 * h + 1] = a.y - bv.y;
-                    if (nt0 == 0) {
-                        sre += sv[2 * h];
-                        sim += sv[2 * h + 1];
-                    }
-                }
-                unsigned sh[4], sl[4], dh[4], dl[4];
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    ptc::split_tf32(sv[e], sh[e], sl[e]);
-                    ptc::split_tf32(dv[e], dh[e], dl[e]);
-                }
-                const bool ja = 8 * ks + t + 1 <= H, jb = 8 * ks + t + 5 <= H;
-#pragma unroll
-                for (int n = 0; n < NTC; ++n) {
-                    if (nt0 + n < KS) { // warp-uniform
-                        const bool kin = 8 * (nt0 + n) + g + 1 <= H;
-                        const float2 ca = (kin && ja) ? wtab[qa[n]] : make_float2(0.f, 0.f);
-                        const float2 cb = (kin && jb) ? wtab[qb[n]] : make_float2(0.f, 0.f);
-                        unsigned ch0, cl0, ch1, cl1, sh0, sl0, sh1, sl1;
-                        ptc::split_tf32(ca.x, ch0, cl0);
-                        ptc::split_tf32(cb.x, ch1, cl1);
-                        ptc::split_tf32(ca.y, sh0, sl0);
-                        ptc::split_tf32(cb.y, sh1, sl1);
-                        ptc::mma_tf32(u[n], sl, ch0, ch1);
-                        ptc::mma_tf32(u[n], sh, cl0, cl1);
-                        ptc::mma_tf32(u[n], sh, ch0, ch1);
-                        ptc::mma_tf32(w[n], dl, sh0, sh1);
-                        ptc::mma_tf32(w[n], dh, sl0, sl1);
-                        ptc::mma_tf32(w[n], dh, sh0, sh1);
-                    }
-                    qa[n] += step[n];
-                    qa[n] -= qa[n] >= P ? P : 0;
-                    qb[n] += step[n];
-                    qb[n] -= qb[n] >= P ? P : 0;
-                }
-            }
-            if (nt0 == 0) {
-                sre += __shfl_xor_sync(0xffffffffu, sre, 1);
-                sim += __shfl_xor_sync(0xffffffffu, sim, 1);
-                sre += __shfl_xor_sync(0xffffffffu, sre, 2);
-                sim += __shfl_xor_sync(0xffffffffu, sim, 2);
-                if (valid && t == 0) {
-                    *out(0) = make_float2(x0.x + sre, x0.y + sim);
-                }
-            }
-            if (valid) {
-#pragma unroll
-                for (int n = 0; n < NTC; ++n) {
-#pragma unroll
-                    for (int e = 0; e < 2; ++e) {
-                        const int k = 8 * (nt0 + n) + 2 * t + 1 + e;
-                        if (nt0 + n < KS && k <= H) {
-                            const float ur = u[n][e], ui = u[n][2 + e];
-                            const float wr = w[n][e], wi = w[n][2 + e];
-                            *out(k) = make_float2(x0.x + ur - wi, x0.y + ui + wr);
-                            *out(P - k) = make_float2(x0.x + ur + wi, x0.y + ui - wr);
-                        }
-                    }
-                }
-            }
-        }
-    }
-}
 #endif
 
 template <class R, int Kind, class IO>
@@ -508,15 +364,6 @@ __device__ __forceinline__ void run_stage_generic(const transform_ctx<R, Kind, I
         for (int q = threadIdx.x; q < P; q += blockDim.x) {
             wtab[q] = __ldg(tw + q * wstride);
         }
-#ifndef GBFFT_NVRTC
-        if constexpr (sizeof(R) == 4) {
-            if (!dst_g) {
-                __syncthreads(); // the w_P table is complete
-                run_stage_bigprime_tc(c, P, Ns, src_buf, dst_buf, reinterpret_cast<const float2 *>(wtab));
-                return;
-            }
-        }
-#endif
     }
     if (Ns > 1) {
         const int twstride = p.Nt / (Ns * P);

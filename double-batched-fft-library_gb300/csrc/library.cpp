@@ -301,11 +301,6 @@ static bool ptc_supported_host(int P) {
 // and every warp of the block must be full.  NVRTC kernels (user callbacks) keep the
 // CUDA-core stage and its table.
 static bool tc_prime(int prec, int P) { return prec == 4 && ptc_supported_host(P); }
-// Float odd radices above 61 (the runtime engine's generic stage) also run on the tensor
-// cores, reading their coefficients from the shared w_P table: full warps, shared source
-// and destination (a copy stage follows when the radix is the last one).
-static bool tc_big_prime(int prec, int P) { return prec == 4 && !unrolled(P) && P % 2 == 1 && P > gen_table_max_p; }
-static bool tc_any(int prec, int P) { return tc_prime(prec, P) || tc_big_prime(prec, P); }
 // shared-memory elements the generic stage of radix P needs after the data buffers
 // (`tc_ok`: the kernel has the tensor-core stages, i.e. it is not an NVRTC kernel)
 static int gen_shared_elems(int prec, int P, bool tc_ok) {
@@ -990,7 +985,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     }
     // the compile-time prime stages write shared memory only, so a prime last stage is
     // followed by a copy stage (the same radices for the runtime engine)
-    if (!post && (table_generic(rad.back()) || tc_big_prime(q.prec, rad.back()))) {
+    if (!post && table_generic(rad.back())) {
         rad.push_back(1);
     }
     // real transforms must finish all global reads of a tile before the first global write
@@ -1204,7 +1199,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     }
     ps.grid = static_cast<unsigned>(p.m_tiles * k_tiles);
     ps.block = static_cast<unsigned>((Mb / V) * T * Kb);
-    if (!has_cb && std::any_of(rad.begin(), rad.end(), [&](int r) { return tc_any(q.prec, r); })) {
+    if (!has_cb && std::any_of(rad.begin(), rad.end(), [&](int r) { return tc_prime(q.prec, r); })) {
         // tensor-core prime stages run on full warps; the extra threads only take part in
         // the barriers (both engines support threads beyond the tile)
         ps.block = (ps.block + 31) / 32 * 32;
@@ -1314,7 +1309,7 @@ const char *plan_pass_fixed(int prec, int type, int dir, long long M, long long 
     // a generic odd-radix stage reads and writes shared memory only (its tensor-core form
     // writes the butterflies of several transforms per warp): a copy stage follows it, as
     // in make_1d_pass
-    if (!post && (table_generic(rad[L - 1]) || tc_big_prime(prec, rad[L - 1]))) {
+    if (!post && table_generic(rad[L - 1])) {
         if (L >= max_stages) {
             return "too many stages";
         }
@@ -1417,7 +1412,7 @@ const char *plan_pass_fixed(int prec, int type, int dir, long long M, long long 
     grid = static_cast<unsigned>(p.m_tiles * k_tiles);
     block = static_cast<unsigned>(Mb * T * Kb);
     for (int i = 0; i < L; ++i) {
-        if (tc_any(prec, rad[i])) { // tensor-core prime stages run on full warps
+        if (tc_prime(prec, rad[i])) { // tensor-core prime stages run on full warps
             block = (block + 31) / 32 * 32;
             break;
         }
@@ -2444,8 +2439,12 @@ int bbfft_ragged_execute(bbfft_ragged_t ragged, cudaStream_t stream, int use_gra
         if (!ragged->exec && ragged->form == BBFFT_RAGGED_CLASSES) {
             // one kernel node per class in kChains chains (largest classes first, dealt
             // round robin): the chains run concurrently, the kernels of a chain back to back
-            // (hundreds of independent nodes measured slower than a few chains)
-            constexpr std::size_t kChains = 4;
+            // (hundreds of independent nodes measured slower than a few chains);
+            // BBFFT_GB300_RAGGED_CHAINS overrides the number of chains
+            std::size_t kChains = 4;
+            if (const char *e = std::getenv("BBFFT_GB300_RAGGED_CHAINS")) {
+                kChains = std::max<std::size_t>(1, std::strtoul(e, nullptr, 10));
+            }
             GB_CUDA(cudaGraphCreate(&ragged->graph, 0));
             const void *items = ragged->items->ptr;
             std::vector<std::size_t> order(ragged->classes.size());
