@@ -30,7 +30,8 @@ PROBES_LIB = os.path.join(OUTDIR, 'libbbfft_probes.so')
 
 ARCH = '-gencode=arch=compute_103a,code=sm_103a'
 ENGINE_HEADERS = ['params.h', 'root_of_unity_table.cuh', 'radix.cuh', 'engine.cuh']
-KERNEL_UNITS = ['kernels_f32.cu', 'kernels_f64.cu', 'noalloc.cu', 'tc.cu', 'strided_copy.cu']
+KERNEL_UNITS = ['kernels_f32.cu', 'kernels_f64.cu', 'noalloc.cu', 'tc.cu', 'strided_copy.cu',
+                'bluestein.cu']
 # relocatable device code, linked with nvcc -dlink: the persistent ragged kernel calls the
 # compile-time-size tile functions of the generated ragged_ct_<i>.cu units
 RDC_UNITS = ['ragged.cu']

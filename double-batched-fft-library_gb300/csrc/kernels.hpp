@@ -32,6 +32,9 @@ extern const ct_entry cover_ct_table[];
 int cover_ct_lookup(int prec, int kind, int nc, int T, const int *rad, int L);
 const void *cover_ct_kernel(int i);
 
+// Bluestein's algorithm for float lengths with a prime factor above 61 (bluestein.cu)
+const void *bluestein_kernel(int kind);
+
 // tensor-core DFT stages (tc.cu)
 const void *tc_kernel(int pieces, int nc);
 std::size_t tc_shared_bytes();

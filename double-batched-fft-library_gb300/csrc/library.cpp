@@ -398,6 +398,7 @@ struct pass {
     const void *func = nullptr;
     std::shared_ptr<module> mod;
     std::shared_ptr<device_buffer> tw;
+    std::shared_ptr<device_buffer> extra; // Bluestein tables (chirp, FFT of the chirp, w_L)
     bool inplace_ok = true;
     bool specialized = false; // compile-time-size kernel
     bool tc = false;          // tensor-core DFT stages
@@ -877,6 +878,136 @@ int callback_io(const char *load_fn, const char *store_fn) {
     return ((load_fn && *load_fn) ? 1 : 0) | ((store_fn && *store_fn) ? 2 : 0);
 }
 
+static int largest_prime_factor(int n) {
+    int f = 1;
+    for (int p = 2; n > 1;) {
+        if (n % p == 0) {
+            f = p;
+            n /= p;
+        } else {
+            ++p;
+        }
+    }
+    return f;
+}
+
+// Bluestein pass (bluestein.cu) for a float length Nc whose largest prime factor is above
+// 61: one CTA per tile of Mb x Kb transforms (4 per CTA, 64 threads each), the convolution
+// of length L (the power of two >= 2 Nc - 1) in shared memory.  Tables in long double,
+// rounded once: chirp c_n = exp(-i pi (n^2 mod 2 Nc) / Nc), FFT_L(b) / L with b_m =
+// conj(c_|m|) at m mod L, and w_L^{-i}.
+static pass make_bluestein_pass(pass_request const &q, pass ps, int flags, int N, int Nc, int Nt,
+                                int device) {
+    int L = 128;
+    while (L < 2 * Nc - 1) {
+        L *= 2;
+    }
+    long long const M = q.M, K = q.K;
+    int const Mb = static_cast<int>(std::min<long long>(M, 4));
+    int const Kb = static_cast<int>(std::max<long long>(1, std::min<long long>(4 / Mb, K)));
+    fft_params &p = ps.p;
+    p.M = M;
+    p.K = K;
+    if ((N + 1) * std::max(std::llabs(q.is1), std::llabs(q.os1)) > 0x7fffffffLL) {
+        bad_config("stride of the FFT mode too large");
+    }
+    p.is1 = static_cast<int>(q.is1);
+    p.is2 = q.is2;
+    p.os1 = static_cast<int>(q.os1);
+    p.os2 = q.os2;
+    p.N = N;
+    p.Nc = Nc;
+    p.Nt = Nt;
+    p.L = 0;
+    p.T = 64;
+    p.Mb = Mb;
+    p.Kb = Kb;
+    p.m_tiles = static_cast<int>((M + Mb - 1) / Mb);
+    p.flags = flags;
+    if (ps.kind == kind_r2c_half && q.is1 == 1 && M == 1 && q.is2 % 2 == 0) {
+        p.flags |= flag_vec_in;
+    }
+    if (ps.kind == kind_c2r_half && q.os1 == 1 && M == 1 && q.os2 % 2 == 0) {
+        p.flags |= flag_vec_out;
+    }
+    p.nbuf = 1;
+    p.buf_elems = Mb * Kb * L;
+    p.pad_shift = 30;
+    p.pad_add = 0;
+    p.sw_a = 30;
+    p.scale = 1.0;
+    p.bL = L;
+    ps.tw = get_twiddles(device, 4, Nt);
+    p.tw = ps.tw->ptr;
+    std::vector<float> h(2 * static_cast<std::size_t>(Nc + 2 * L));
+    long double const pi = 3.141592653589793238462643383279502884L;
+    std::vector<long double> cr(Nc), ci(Nc);
+    for (int n = 0; n < Nc; ++n) {
+        long long const qn = (static_cast<long long>(n) * n) % (2LL * Nc);
+        long double const a = pi * static_cast<long double>(qn) / static_cast<long double>(Nc);
+        cr[n] = std::cos(a);
+        ci[n] = -std::sin(a);
+        h[2 * n] = static_cast<float>(cr[n]);
+        h[2 * n + 1] = static_cast<float>(ci[n]);
+    }
+    std::vector<long double> wc(L), ws(L); // w_L^{-i} = (cos, -sin)(2 pi i / L)
+    for (int i = 0; i < L; ++i) {
+        long double c, sn;
+        twiddle_value(i, L, c, sn);
+        wc[i] = c;
+        ws[i] = -sn;
+        h[2 * (Nc + L + i)] = static_cast<float>(c);
+        h[2 * (Nc + L + i) + 1] = static_cast<float>(-sn);
+    }
+    std::vector<long double> br(L, 0.0L), bi(L, 0.0L);
+    for (int m = 0; m < Nc; ++m) { // b_m = conj(c_m) at m and at L - m
+        br[m] = cr[m];
+        bi[m] = -ci[m];
+        if (m > 0) {
+            br[L - m] = cr[m];
+            bi[L - m] = -ci[m];
+        }
+    }
+    for (int k = 0; k < L; ++k) {
+        long double sr = 0.0L, si = 0.0L;
+        for (int m = 0; m < L; ++m) {
+            if (br[m] == 0.0L && bi[m] == 0.0L) {
+                continue;
+            }
+            int const e = static_cast<int>((static_cast<long long>(m) * k) % L);
+            sr += br[m] * wc[e] - bi[m] * ws[e];
+            si += br[m] * ws[e] + bi[m] * wc[e];
+        }
+        h[2 * (Nc + k)] = static_cast<float>(sr / L);
+        h[2 * (Nc + k) + 1] = static_cast<float>(si / L);
+    }
+    ps.extra = std::make_shared<device_buffer>(h.size() * sizeof(float));
+    GB_CUDA(cudaMemcpy(ps.extra->ptr, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+    p.bs = ps.extra->ptr;
+    long long const k_tiles = (K + Kb - 1) / Kb;
+    if (static_cast<long long>(p.m_tiles) * k_tiles > 0x7fffffffLL) {
+        bad_config("tensor too large for one launch");
+    }
+    ps.grid = static_cast<unsigned>(p.m_tiles * k_tiles);
+    ps.block = static_cast<unsigned>(Mb * 64 * Kb);
+    ps.smem = static_cast<std::size_t>(p.buf_elems) * 8;
+    ps.V = 1;
+    ps.inplace_ok = q.type == BBFFT_C2C || Mb >= M;
+    ps.func = bluestein_kernel(ps.kind);
+    if (!ps.func) {
+        throw status_error(BBFFT_INTERNAL_ERROR, "Bluestein kernel not found");
+    }
+    if (needs_smem_optin(ps.smem)) {
+        allow_max_smem(ps.func, device);
+    }
+    std::ostringstream id;
+    id << "gbfft_f32_" << kind_name(ps.kind) << "_fl" << flags << "_bluestein_L" << L << "_M" << M
+       << "_N" << N << "_Mb" << Mb << "_Kb" << Kb << "_is" << q.is1 << "_" << q.is2 << "_os" << q.os1
+       << "_" << q.os2;
+    ps.identifier = c_ident(id.str());
+    return ps;
+}
+
 pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     pass ps;
     ps.prec = q.prec;
@@ -912,6 +1043,12 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     }
     int Nc = (is_real && even) ? N / 2 : N;
     int Nt = (is_real && even) ? N : Nc;
+    // float lengths with a prime factor above 61: Bluestein's algorithm in one kernel
+    bool const has_cb0 = (q.load_fn && *q.load_fn) || (q.store_fn && *q.store_fn);
+    if (q.prec == 4 && !has_cb0 && !q.runtime_only && q.compute == BBFFT_COMPUTE_NATIVE &&
+        q.radices.empty() && q.T == 0 && largest_prime_factor(Nc) > gen_table_max_p) {
+        return make_bluestein_pass(q, ps, flags, N, Nc, Nt, device);
+    }
 
     // autotuned blocking (radices, threads per transform, V, Mb, Kb, register budget)
     tune_entry const *te = nullptr;
