@@ -931,9 +931,10 @@ static pass make_bluestein_pass(pass_request const &q, pass ps, int flags, int N
         p.flags |= flag_vec_out;
     }
     p.nbuf = 1;
-    p.buf_elems = Mb * Kb * L;
-    p.pad_shift = 30;
-    p.pad_add = 0;
+    // one spare element per 16: the radix-4 stages write with strides of 4^s elements
+    p.pad_shift = 4;
+    p.pad_add = 1;
+    p.buf_elems = Mb * Kb * L + (Mb * Kb * L >> 4) + 1;
     p.sw_a = 30;
     p.scale = 1.0;
     p.bL = L;
