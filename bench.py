@@ -985,6 +985,10 @@ def run_profile(args):
         assert nin <= x.numel() and nout <= y.numel()
         plan = bb.Plan(cfg, stream=stream)
         plan.execute(x.data_ptr(), y.data_ptr())
+        i = plan.info()
+        print('plan', i.identifier.decode(), 'T', i.threads_per_transform, 'Mb', i.mb, 'Kb', i.kb,
+              'V', i.vector_width, 'block', i.block_threads, 'smem', i.shared_bytes,
+              'min_blocks', i.min_blocks)
     torch.cuda.synchronize()
     print('profiled launches:', len(cases))
 

@@ -34,6 +34,7 @@ const void *cover_ct_kernel(int i);
 
 // Bluestein's algorithm for float lengths with a prime factor above 61 (bluestein.cu)
 const void *bluestein_kernel(int kind);
+int bluestein_threads(int L); // threads per transform of the length-L tile
 
 // tensor-core DFT stages (tc.cu)
 const void *tc_kernel(int pieces, int nc);

@@ -898,13 +898,19 @@ static int largest_prime_factor(int n) {
 // conj(c_|m|) at m mod L, and w_L^{-i}.
 static pass make_bluestein_pass(pass_request const &q, pass ps, int flags, int N, int Nc, int Nt,
                                 int device) {
-    int L = 128;
+    int L = 256;
     while (L < 2 * Nc - 1) {
         L *= 2;
     }
+    if (L > 1024) {
+        throw status_error(BBFFT_INTERNAL_ERROR, "Bluestein length above 1024");
+    }
+    // T threads per transform, 256 threads per tile
+    int const T = bluestein_threads(L);
     long long const M = q.M, K = q.K;
     int const Mb = static_cast<int>(std::min<long long>(M, 4));
-    int const Kb = static_cast<int>(std::max<long long>(1, std::min<long long>(4 / Mb, K)));
+    int const Kb =
+        static_cast<int>(std::max<long long>(1, std::min<long long>(256 / T / Mb, K)));
     fft_params &p = ps.p;
     p.M = M;
     p.K = K;
@@ -919,7 +925,7 @@ static pass make_bluestein_pass(pass_request const &q, pass ps, int flags, int N
     p.Nc = Nc;
     p.Nt = Nt;
     p.L = 0;
-    p.T = 64;
+    p.T = T;
     p.Mb = Mb;
     p.Kb = Kb;
     p.m_tiles = static_cast<int>((M + Mb - 1) / Mb);
@@ -931,10 +937,13 @@ static pass make_bluestein_pass(pass_request const &q, pass ps, int flags, int N
         p.flags |= flag_vec_out;
     }
     p.nbuf = 1;
-    // one spare element per 16: the radix-4 stages write with strides of 4^s elements
+    // spare elements after every 16: the stages write with strides of Ns * Mb elements;
+    // these gaps (searched per L and Mb with a model of the 32 banks, 8-byte elements in
+    // half-warp phases) leave one wavefront per 16 lanes except for L = 512, Mb = 1 (+20 %)
+    int const E = Mb * Kb * L;
     p.pad_shift = 4;
-    p.pad_add = 1;
-    p.buf_elems = Mb * Kb * L + (Mb * Kb * L >> 4) + 1;
+    p.pad_add = L == 512 && Mb % 2 == 0 ? 2 : 1;
+    p.buf_elems = E + (E >> 4) * p.pad_add + p.pad_add;
     p.sw_a = 30;
     p.scale = 1.0;
     p.bL = L;
@@ -990,7 +999,7 @@ static pass make_bluestein_pass(pass_request const &q, pass ps, int flags, int N
         bad_config("tensor too large for one launch");
     }
     ps.grid = static_cast<unsigned>(p.m_tiles * k_tiles);
-    ps.block = static_cast<unsigned>(Mb * 64 * Kb);
+    ps.block = static_cast<unsigned>(Mb * T * Kb);
     ps.smem = static_cast<std::size_t>(p.buf_elems) * 8;
     ps.V = 1;
     ps.inplace_ok = q.type == BBFFT_C2C || Mb >= M;

@@ -365,8 +365,8 @@ def test_prime_factor_lengths(bb, po, torch_cuda, type):
     print('worst rel-L2', worst)
 
 
-# every length up to 512 with a prime factor above 61 (tensor-core stage with coefficients
-# from the w_P table, runtime-size engine)
+# every length up to 512 with a prime factor above 61 (float: the Bluestein kernel, one
+# shared-memory layout per transforms-per-tile count Mb = 1..4)
 BIG_PRIME_N = [n for n in range(67, 513) if _largest_prime_factor(n) > 61]
 
 
@@ -378,7 +378,7 @@ def test_big_prime_factor_lengths(bb, po, torch_cuda, type):
     rng = np.random.default_rng(21 + type)
     worst = 0.0
     for N in BIG_PRIME_N:
-        M = int(rng.choice([1, 2, 8, 16]))
+        M = int(rng.choice([1, 2, 3, 8, 16]))
         K = int(rng.integers(1, 12))
         d = bb.BACKWARD if type == 2 else (bb.FORWARD if type == 1 else
                                            int(rng.choice([bb.FORWARD, bb.BACKWARD])))
