@@ -12,7 +12,13 @@
 // The two length-L transforms are Stockham stages of radix 16 / 8 / 4 (256 = 16 x 16 on 16
 // threads per transform, 512 = 8 x 8 x 8 and 1024 = 16 x 16 x 4 on 64) exchanging through
 // shared memory; each thread holds its butterflies in registers across the barrier of an
-// in-place stage.  The steps around them are fused into the first and last stages:
+// in-place stage.  The twiddles of the stages after the first are a table of the plan laid
+// out per stage as [r - 1][b mod Ns] (consecutive butterflies read consecutive entries:
+// no bank conflicts), which each CTA copies into shared memory (at most 1008 entries; the
+// scattered twiddle reads from global memory cost a sector each).  A tile loop over
+// persistent CTAs was not kept: it held the per-thread addresses of every stage across the
+// loop and spilled.  The steps around the transforms are fused into the first
+// and last stages:
 // - the first stage of the forward transform loads its butterfly's inputs from global
 //   memory (the kind's own load: c2c, the real even / odd forms, the reference's c2r
 //   pre-process; engine.cuh gload) and multiplies them by the chirp; inputs at n >= L / 2
@@ -37,18 +43,23 @@ __host__ __device__ constexpr int stages_of(int L) { return L == 256 ? 2 : 3; }
 __host__ __device__ constexpr int span_of(int L, int s) { // product of the radices before s
     return s == 0 ? 1 : span_of(L, s - 1) * radix_of(L, s - 1);
 }
+// offset of stage s's twiddles ((R - 1) Ns entries from stage 1 on) and the table size
+__host__ __device__ constexpr int tw_offset(int L, int s) {
+    return s <= 1 ? 0 : tw_offset(L, s - 1) + (radix_of(L, s - 1) - 1) * span_of(L, s - 1);
+}
+__host__ __device__ constexpr int tw_entries(int L) { return tw_offset(L, stages_of(L)); }
 
 // One radix-R Stockham stage of the length-L transform on T threads per transform, the
 // earlier stages spanning Ns: butterfly b reads elements b + r L / R (times the twiddles
-// w_L^{-r (b mod Ns) L / (Ns R)}) and writes (b / Ns) Ns R + (b mod Ns) + r Ns.
-// `load(n)` / `store(n, v)` move element n; `HALF_IN`: inputs at r >= R / 2 are zero;
-// `HALF_OUT`: outputs at r >= R / 2 are not needed; `MID`: barrier between the loads and
-// the stores (in-place shared-memory stage).  Threads beyond the tile hold j = 1 << 20.
+// w_L^{-r (b mod Ns) L / (Ns R)} = tw[(r - 1) Ns + b mod Ns]) and writes
+// (b / Ns) Ns R + (b mod Ns) + r Ns.  `load(n)` / `store(n, v)` move element n; `HALF_IN`:
+// inputs at r >= R / 2 are zero; `HALF_OUT`: outputs at r >= R / 2 are not needed; `MID`:
+// barrier between the loads and the stores (in-place shared-memory stage).  Threads
+// beyond the tile hold j = 1 << 20.
 template <int L, int T, int R, int Ns, bool HALF_IN, bool HALF_OUT, bool MID, class Load, class Store>
-__device__ __forceinline__ void stage(int j, const float2 *__restrict__ wL, Load load, Store store) {
+__device__ __forceinline__ void stage(int j, const float2 *tw, Load load, Store store) {
     constexpr int nb = L / R;
     constexpr int IT = (nb + T - 1) / T;
-    constexpr int tws = L / (Ns * R);
     float2 v[IT][R];
 #pragma unroll
     for (int it = 0; it < IT; ++it) {
@@ -61,7 +72,7 @@ __device__ __forceinline__ void stage(int j, const float2 *__restrict__ wL, Load
                 if (!HALF_IN || r < R / 2) {
                     x = load(b + r * nb);
                     if (Ns > 1 && r > 0) {
-                        x = cmul(x, __ldg(wL + r * kk * tws));
+                        x = cmul(x, tw[(r - 1) * Ns + kk]);
                     }
                 }
                 v[it][r] = x;
@@ -87,82 +98,137 @@ __device__ __forceinline__ void stage(int j, const float2 *__restrict__ wL, Load
 
 // Middle stages s = 1 .. S - 2 of a transform, shared memory to shared memory.
 template <int L, int s, class SmLoad, class SmStore>
-__device__ __forceinline__ void middle(int j, const float2 *wL, SmLoad ld, SmStore st) {
+__device__ __forceinline__ void middle(int j, const float2 *tw, SmLoad ld, SmStore st) {
     if constexpr (s < stages_of(L) - 1) {
-        stage<L, threads_of(L), radix_of(L, s), span_of(L, s), false, false, true>(j, wL, ld, st);
+        stage<L, threads_of(L), radix_of(L, s), span_of(L, s), false, false, true>(
+            j, tw + tw_offset(L, s), ld, st);
         __syncthreads();
-        middle<L, s + 1>(j, wL, ld, st);
+        middle<L, s + 1>(j, tw, ld, st);
     }
 }
 
-template <int Kind, int L> __device__ __forceinline__ void tile(const fft_params &p) {
+// PAIR (odd real N, no adjoint weights): one complex transform serves the real transforms
+// k0 = 2k and k0 + 1 of the tile's pair index k.  r2c: z = x_k0 + i x_k0+1, and with
+// Z = FFT(z), X_k0[k] = (Z_k + conj Z_{N-k}) / 2, X_k0+1[k] = -i (Z_k - conj Z_{N-k}) / 2.
+// c2r: the engine's load gives A = conj X_k0 and B = conj X_k0+1 (Hermitian extensions),
+// the forward transform of A - i B is x_k0 - i x_k0+1.
+template <int Kind, int L, bool PAIR>
+__device__ __forceinline__ void tile(const fft_params &p, long long t, const float2 *tw) {
     constexpr int T = threads_of(L);
     constexpr int S = stages_of(L);
     constexpr int R0 = radix_of(L, 0);
     constexpr int RL = radix_of(L, S - 1);
     constexpr int NL = span_of(L, S - 1);
+    const float2 *twl = tw + tw_offset(L, S - 1); // last stage's twiddles
     extern __shared__ __align__(16) unsigned char smem_raw[];
     int j;
-    auto c = make_ctx<float, Kind, default_io>(p, smem_raw, T, L, j, blockIdx.x);
+    auto c = make_ctx<float, Kind, default_io>(p, smem_raw, T, L, j, t);
+    auto c2 = c; // the second transform of a pair
+    if constexpr (PAIR) {
+        const int m_l = threadIdx.x % p.Mb;
+        const int k_l = threadIdx.x / (p.Mb * T);
+        const long long m = (t % p.m_tiles) * p.Mb + m_l;
+        const long long k0 = 2 * ((t / p.m_tiles) * p.Kb + k_l);
+        c.ib = m + k0 * p.is2;
+        c.ob = m + k0 * p.os2;
+        c.active = m < p.M && k0 < p.K && k_l < p.Kb;
+        c2.ib = c.ib + p.is2;
+        c2.ob = c.ob + p.os2;
+        c2.active = c.active && k0 + 1 < p.K;
+    }
     const int Nc = p.Nc;
     const float2 *chirp = static_cast<const float2 *>(p.bs);
     const float2 *bhat = chirp + Nc;
-    const float2 *wL = bhat + L;
     auto sm_load = [&](int n) { return c.sm[c.sidx(0, n)]; };
     auto sm_store = [&](int n, float2 v) { c.sm[c.sidx(0, n)] = v; };
     // forward transform of a = x . chirp: first stage from global memory
     auto g_load = [&](int n) {
         float2 v = make_float2(0.f, 0.f);
         if (n < Nc && c.active) {
-            v = cmul(c.template gload<0>(n), __ldg(chirp + n));
+            v = c.template gload<0>(n);
+            if constexpr (PAIR) {
+                const float2 b = c2.active ? c2.template gload<0>(n) : make_float2(0.f, 0.f);
+                v = Kind == kind_r2c_full ? make_float2(v.x, b.x) : make_float2(v.x + b.y, v.y - b.x);
+            }
+            v = cmul(v, __ldg(chirp + n));
         }
         return v;
     };
-    stage<L, T, R0, 1, true, false, false>(j, wL, g_load, sm_store);
+    stage<L, T, R0, 1, true, false, false>(j, tw, g_load, sm_store);
     __syncthreads();
-    middle<L, 1>(j, wL, sm_load, sm_store);
+    middle<L, 1>(j, tw, sm_load, sm_store);
     // last forward stage: times FFT(b) / L, conjugated for the inverse transform
     auto mul_store = [&](int n, float2 v) {
         v = cmul(v, __ldg(bhat + n));
         c.sm[c.sidx(0, n)] = make_float2(v.x, -v.y);
     };
-    stage<L, T, RL, NL, false, false, true>(j, wL, sm_load, mul_store);
+    stage<L, T, RL, NL, false, false, true>(j, twl, sm_load, mul_store);
     __syncthreads();
     // inverse transform (of the conjugate)
-    stage<L, T, R0, 1, false, false, true>(j, wL, sm_load, sm_store);
+    stage<L, T, R0, 1, false, false, true>(j, tw, sm_load, sm_store);
     __syncthreads();
-    middle<L, 1>(j, wL, sm_load, sm_store);
-    if constexpr (Kind == kind_r2c_half) {
+    middle<L, 1>(j, tw, sm_load, sm_store);
+    if constexpr (Kind == kind_r2c_half || (PAIR && Kind == kind_r2c_full)) {
         // Z_k = c_k conj(y_k) into shared memory, then the r2c post-process
         auto z_store = [&](int k, float2 y) {
             if (k < Nc) {
                 c.sm[c.sidx(0, k)] = cmul(make_float2(y.x, -y.y), __ldg(chirp + k));
             }
         };
-        stage<L, T, RL, NL, false, true, true>(j, wL, sm_load, z_store);
+        stage<L, T, RL, NL, false, true, true>(j, twl, sm_load, z_store);
         __syncthreads();
-        r2c_post<0, T>(c, j, 0);
+        if constexpr (Kind == kind_r2c_half) {
+            r2c_post<0, T>(c, j, 0);
+        } else if (c.active) {
+            // split the spectra of the two real transforms
+            for (int k = j; 2 * k <= Nc; k += T) {
+                const float2 zk = c.sm[c.sidx(0, k)];
+                const float2 zn = c.sm[c.sidx(0, k == 0 ? 0 : Nc - k)];
+                c.template gstore<0>(k, make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y)));
+                if (c2.active) {
+                    c2.template gstore<0>(k, make_float2(0.5f * (zk.y + zn.y), 0.5f * (zn.x - zk.x)));
+                }
+            }
+        }
     } else {
         auto g_store = [&](int k, float2 y) {
             if (k < Nc && c.active) {
-                c.template gstore<0>(k, cmul(make_float2(y.x, -y.y), __ldg(chirp + k)));
+                const float2 v = cmul(make_float2(y.x, -y.y), __ldg(chirp + k));
+                c.template gstore<0>(k, v);
+                if constexpr (PAIR) {
+                    if (c2.active) {
+                        c2.template gstore<0>(k, make_float2(-v.y, 0.f));
+                    }
+                }
             }
         };
-        stage<L, T, RL, NL, false, true, false>(j, wL, sm_load, g_store);
+        stage<L, T, RL, NL, false, true, false>(j, twl, sm_load, g_store);
     }
 }
 
-template <int Kind>
+// One tile per CTA; the stage twiddles are copied into shared memory after the tile buffer
+template <int Kind, int L, bool PAIR> __device__ __forceinline__ void tiles(const fft_params &p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *tw = reinterpret_cast<float2 *>(smem_raw) + p.buf_elems;
+    const float2 *gtw = static_cast<const float2 *>(p.bs) + p.Nc + L;
+    for (int i = threadIdx.x; i < tw_entries(L); i += blockDim.x) {
+        tw[i] = __ldg(gtw + i);
+    }
+    __syncthreads();
+    tile<Kind, L, PAIR>(p, blockIdx.x, tw);
+}
+
+template <int Kind, bool PAIR>
 __global__ void __launch_bounds__(256, 4) bluestein_kernel(const __grid_constant__ fft_params p) {
     switch (p.bL) {
     case 256:
-        tile<Kind, 256>(p);
+        tiles<Kind, 256, PAIR>(p);
         break;
     case 512:
-        tile<Kind, 512>(p);
+        tiles<Kind, 512, PAIR>(p);
         break;
     case 1024:
-        tile<Kind, 1024>(p);
+        tiles<Kind, 1024, PAIR>(p);
         break;
     }
 }
@@ -170,19 +236,23 @@ __global__ void __launch_bounds__(256, 4) bluestein_kernel(const __grid_constant
 } // namespace blu
 
 int bluestein_threads(int L) { return blu::threads_of(L); }
+int bluestein_stages(int L) { return blu::stages_of(L); }
+int bluestein_radix(int L, int s) { return blu::radix_of(L, s); }
 
-const void *bluestein_kernel(int kind) {
+const void *bluestein_kernel(int kind, bool pair) {
     switch (kind) {
     case kind_c2c:
-        return reinterpret_cast<const void *>(&blu::bluestein_kernel<kind_c2c>);
+        return reinterpret_cast<const void *>(&blu::bluestein_kernel<kind_c2c, false>);
     case kind_r2c_half:
-        return reinterpret_cast<const void *>(&blu::bluestein_kernel<kind_r2c_half>);
+        return reinterpret_cast<const void *>(&blu::bluestein_kernel<kind_r2c_half, false>);
     case kind_r2c_full:
-        return reinterpret_cast<const void *>(&blu::bluestein_kernel<kind_r2c_full>);
+        return pair ? reinterpret_cast<const void *>(&blu::bluestein_kernel<kind_r2c_full, true>)
+                    : reinterpret_cast<const void *>(&blu::bluestein_kernel<kind_r2c_full, false>);
     case kind_c2r_half:
-        return reinterpret_cast<const void *>(&blu::bluestein_kernel<kind_c2r_half>);
+        return reinterpret_cast<const void *>(&blu::bluestein_kernel<kind_c2r_half, false>);
     case kind_c2r_full:
-        return reinterpret_cast<const void *>(&blu::bluestein_kernel<kind_c2r_full>);
+        return pair ? reinterpret_cast<const void *>(&blu::bluestein_kernel<kind_c2r_full, true>)
+                    : reinterpret_cast<const void *>(&blu::bluestein_kernel<kind_c2r_full, false>);
     }
     return nullptr;
 }

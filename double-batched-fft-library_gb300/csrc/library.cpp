@@ -398,7 +398,7 @@ struct pass {
     const void *func = nullptr;
     std::shared_ptr<module> mod;
     std::shared_ptr<device_buffer> tw;
-    std::shared_ptr<device_buffer> extra; // Bluestein tables (chirp, FFT of the chirp, w_L)
+    std::shared_ptr<device_buffer> extra; // Bluestein tables (chirp, FFT of the chirp, stage twiddles)
     bool inplace_ok = true;
     bool specialized = false; // compile-time-size kernel
     bool tc = false;          // tensor-core DFT stages
@@ -908,9 +908,14 @@ static pass make_bluestein_pass(pass_request const &q, pass ps, int flags, int N
     // T threads per transform, 256 threads per tile
     int const T = bluestein_threads(L);
     long long const M = q.M, K = q.K;
+    // odd real N: two real transforms along K per complex transform (not for the adjoint
+    // forms, whose Hermitian weights the pairing does not apply)
+    bool const pair = (ps.kind == kind_r2c_full || ps.kind == kind_c2r_full) && K >= 2 &&
+                      (flags & (flag_adj_r2c | flag_adj_c2r)) == 0;
+    long long const Kt = pair ? (K + 1) / 2 : K; // transforms along K of the tiles
     int const Mb = static_cast<int>(std::min<long long>(M, 4));
     int const Kb =
-        static_cast<int>(std::max<long long>(1, std::min<long long>(256 / T / Mb, K)));
+        static_cast<int>(std::max<long long>(1, std::min<long long>(256 / T / Mb, Kt)));
     fft_params &p = ps.p;
     p.M = M;
     p.K = K;
@@ -949,7 +954,20 @@ static pass make_bluestein_pass(pass_request const &q, pass ps, int flags, int N
     p.bL = L;
     ps.tw = get_twiddles(device, 4, Nt);
     p.tw = ps.tw->ptr;
-    std::vector<float> h(2 * static_cast<std::size_t>(Nc + 2 * L));
+    // stage twiddles of the length-L transform, per stage s >= 1 as [r - 1][kk]:
+    // w_L^{-r kk L / (Ns R)}, kk < Ns
+    std::vector<int> tw_e;
+    for (int s = 1, Ns = bluestein_radix(L, 0); s < bluestein_stages(L); ++s) {
+        int const R = bluestein_radix(L, s);
+        for (int r = 1; r < R; ++r) {
+            for (int kk = 0; kk < Ns; ++kk) {
+                tw_e.push_back(r * kk * (L / (Ns * R)));
+            }
+        }
+        Ns *= R;
+    }
+    int const TW = static_cast<int>(tw_e.size());
+    std::vector<float> h(2 * static_cast<std::size_t>(Nc + L + TW));
     long double const pi = 3.141592653589793238462643383279502884L;
     std::vector<long double> cr(Nc), ci(Nc);
     for (int n = 0; n < Nc; ++n) {
@@ -966,8 +984,10 @@ static pass make_bluestein_pass(pass_request const &q, pass ps, int flags, int N
         twiddle_value(i, L, c, sn);
         wc[i] = c;
         ws[i] = -sn;
-        h[2 * (Nc + L + i)] = static_cast<float>(c);
-        h[2 * (Nc + L + i) + 1] = static_cast<float>(-sn);
+    }
+    for (int i = 0; i < TW; ++i) {
+        h[2 * (Nc + L + i)] = static_cast<float>(wc[tw_e[i]]);
+        h[2 * (Nc + L + i) + 1] = static_cast<float>(ws[tw_e[i]]);
     }
     std::vector<long double> br(L, 0.0L), bi(L, 0.0L);
     for (int m = 0; m < Nc; ++m) { // b_m = conj(c_m) at m and at L - m
@@ -994,24 +1014,25 @@ static pass make_bluestein_pass(pass_request const &q, pass ps, int flags, int N
     ps.extra = std::make_shared<device_buffer>(h.size() * sizeof(float));
     GB_CUDA(cudaMemcpy(ps.extra->ptr, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
     p.bs = ps.extra->ptr;
-    long long const k_tiles = (K + Kb - 1) / Kb;
+    long long const k_tiles = (Kt + Kb - 1) / Kb;
     if (static_cast<long long>(p.m_tiles) * k_tiles > 0x7fffffffLL) {
         bad_config("tensor too large for one launch");
     }
-    ps.grid = static_cast<unsigned>(p.m_tiles * k_tiles);
     ps.block = static_cast<unsigned>(Mb * T * Kb);
-    ps.smem = static_cast<std::size_t>(p.buf_elems) * 8;
+    ps.smem = static_cast<std::size_t>(p.buf_elems + TW) * 8; // tile buffer + stage twiddles
     ps.V = 1;
     ps.inplace_ok = q.type == BBFFT_C2C || Mb >= M;
-    ps.func = bluestein_kernel(ps.kind);
+    ps.func = bluestein_kernel(ps.kind, pair);
     if (!ps.func) {
         throw status_error(BBFFT_INTERNAL_ERROR, "Bluestein kernel not found");
     }
     if (needs_smem_optin(ps.smem)) {
         allow_max_smem(ps.func, device);
     }
+    ps.grid = static_cast<unsigned>(p.m_tiles * k_tiles);
     std::ostringstream id;
-    id << "gbfft_f32_" << kind_name(ps.kind) << "_fl" << flags << "_bluestein_L" << L << "_M" << M
+    id << "gbfft_f32_" << kind_name(ps.kind) << "_fl" << flags << "_bluestein_L" << L
+       << (pair ? "_pair" : "") << "_M" << M
        << "_N" << N << "_Mb" << Mb << "_Kb" << Kb << "_is" << q.is1 << "_" << q.is2 << "_os" << q.os1
        << "_" << q.os2;
     ps.identifier = c_ident(id.str());

@@ -53,7 +53,7 @@ struct fft_params {
     int sw_a, sw_b, sw_mask, plane_chunks;
     double scale;          // used with flag_scale_out
     // Bluestein kernels (bluestein.cu): table {chirp (Nc), FFT_L(conj chirp) / L (bL),
-    // w_L^{-i} (bL)} and the convolution length bL (0 for the other kernels)
+    // stage twiddles} and the convolution length bL (0 for the other kernels)
     const void *bs;
     int bL;
 };

@@ -1,9 +1,9 @@
 """CPU emulation of the Bluestein tile (csrc/bluestein.cu) for every length L it runs.
 
 The kernel's stage schedule (radices and threads per transform of each L, the Stockham
-read / write indices, the twiddle index r (b mod Ns) L / (Ns R), the zero upper half of
+read / write indices, the per-stage twiddle table [r - 1][b mod Ns], the zero upper half of
 the first stage's inputs and the unused upper half of the last stage's outputs) and the
-plan's tables (chirp, FFT_L(b) / L, w_L) are restated in numpy and checked against a
+plan's tables (chirp, FFT_L(b) / L, stage twiddles) are restated in numpy and checked against a
 float64 DFT of each complex length Nc with a prime factor above 61 (no GPU)."""
 import numpy as np
 import pytest
@@ -19,29 +19,34 @@ def bluestein_length(nc):
 
 
 def tables(nc, L):
+    """chirp, FFT_L(b) / L and the stage twiddles (per stage s >= 1, [r - 1][kk])."""
     n = np.arange(nc)
     chirp = np.exp(-1j * np.pi * ((n * n) % (2 * nc)) / nc)
     b = np.zeros(L, dtype=complex)
     b[:nc] = np.conj(chirp)
     b[L - nc + 1:] = np.conj(chirp[1:])[::-1]
     bhat = np.fft.fft(b) / L
-    wL = np.exp(-2j * np.pi * np.arange(L) / L)
-    return chirp, bhat, wL
+    radices = SHAPE[L][1]
+    tw, Ns = [], radices[0]
+    for R in radices[1:]:
+        e = np.outer(np.arange(1, R), np.arange(Ns)) * (L // (Ns * R))
+        tw.append(np.exp(-2j * np.pi * e.ravel() / L))
+        Ns *= R
+    return chirp, bhat, [None] + tw
 
 
-def stage(x, L, R, Ns, wL, half_in=False, half_out=False):
+def stage(x, L, R, Ns, tw, half_in=False, half_out=False):
     """One radix-R stage as the kernel runs it (every butterfly b of nb = L / R)."""
     nb = L // R
     b = np.arange(nb)
     kk = b % Ns
-    tws = L // (Ns * R)
     v = np.zeros((nb, R), dtype=complex)
     for r in range(R):
         if half_in and r >= R // 2:
             continue
         t = x[b + r * nb]
         if Ns > 1 and r > 0:
-            t = t * wL[r * kk * tws]
+            t = t * tw[(r - 1) * Ns + kk]
         v[:, r] = t
     V = np.fft.fft(v, axis=1)  # the radix-R butterfly (dft<R>)
     out = np.full(L, np.nan + 0j)
@@ -54,18 +59,18 @@ def stage(x, L, R, Ns, wL, half_in=False, half_out=False):
 def tile(x, nc):
     L = bluestein_length(nc)
     T, radices = SHAPE[L]
-    chirp, bhat, wL = tables(nc, L)
+    chirp, bhat, tw = tables(nc, L)
     a = np.zeros(L, dtype=complex)
     a[:nc] = x * chirp
     # forward transform: first stage from the loads, last stage times bhat, conjugated
     s, Ns = a, 1
     for i, R in enumerate(radices):
-        s = stage(s, L, R, Ns, wL, half_in=(i == 0))
+        s = stage(s, L, R, Ns, tw[i], half_in=(i == 0))
         Ns *= R
     s = np.conj(s * bhat)
     Ns = 1
     for i, R in enumerate(radices):
-        s = stage(s, L, R, Ns, wL, half_out=(i == len(radices) - 1))
+        s = stage(s, L, R, Ns, tw[i], half_out=(i == len(radices) - 1))
         Ns *= R
     return np.conj(s[:nc]) * chirp
 
@@ -107,3 +112,25 @@ def test_every_big_prime_length_quick():
         got = tile(x, nc)
         ref = np.fft.fft(x)
         assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-12, nc
+
+
+@pytest.mark.parametrize('nc', [67, 131, 509])
+def test_paired_real_transforms(nc):
+    """Odd real N: the kernel's two-for-one forms (r2c: z = x0 + i x1, spectra split from
+    Z_k and conj Z_{N-k}; c2r: forward transform of A - i B with A, B the conjugated
+    Hermitian extensions, x0 = Re, x1 = -Im) restated with the emulated tile."""
+    rng = np.random.default_rng(nc + 1)
+    x0, x1 = rng.standard_normal(nc), rng.standard_normal(nc)
+    Z = tile(x0 + 1j * x1, nc)
+    k = np.arange(nc // 2 + 1)
+    zn = Z[(nc - k) % nc]
+    X0 = 0.5 * (Z[k] + np.conj(zn))
+    X1 = -0.5j * (Z[k] - np.conj(zn))
+    assert np.allclose(X0, np.fft.rfft(x0), atol=1e-10)
+    assert np.allclose(X1, np.fft.rfft(x1), atol=1e-10)
+    # c2r: Hermitian extensions of X0, X1, conjugated as the engine's load returns them
+    ext = lambda X: np.concatenate([X, np.conj(X[1:][::-1][:nc - len(X)])])
+    A, B = np.conj(ext(X0)), np.conj(ext(X1))
+    Y = tile(A - 1j * B, nc)
+    assert np.allclose(Y.real, x0 * nc, atol=1e-9)
+    assert np.allclose(-Y.imag, x1 * nc, atol=1e-9)
