@@ -102,7 +102,9 @@ template <int V> __device__ __forceinline__ void stv(double *p, const double *o)
     }
 }
 
-template <class R, int Kind, int NC, int TT, int V, bool MI = false, bool PAIR = false> struct ct_ctx {
+template <class R, int Kind, int NC, int TT, int V, bool MI = false, bool PAIR = false,
+          bool TWO = false>
+struct ct_ctx {
     using C = cplx<R>;
     static constexpr int kind_v = Kind;
     // may_idle: the block has more threads than the tile (persistent ragged kernel); the
@@ -110,6 +112,15 @@ template <class R, int Kind, int NC, int TT, int V, bool MI = false, bool PAIR =
     static constexpr bool may_idle = MI;
     // c2r (even N): form Z[n] and Z[NC-n] together in a pre-pass into shared memory
     static constexpr bool paired_c2r = PAIR;
+    // odd real N (r2c_full / c2r_full): with flag_pair, the real transforms k0 and k0 + 1
+    // (input / output offsets ib, ob and + is2, + os2) share one complex FFT:
+    //   r2c: z = x_k0 + i x_k0+1; X_k0[k] = (Z_k + conj Z_{N-k}) / 2,
+    //        X_k0+1[k] = -i (Z_k - conj Z_{N-k}) / 2 (post-process from shared memory);
+    //   c2r: the forward FFT of A - i B (A, B: the conjugated Hermitian extensions the
+    //        load forms) is x_k0 - i x_k0+1.
+    // Without the flag a TWO tile runs single transforms (r2c still through the
+    // post-process, which then returns Z_k).
+    static constexpr bool two = TWO && (Kind == kind_r2c_full || Kind == kind_c2r_full);
     static constexpr bool half = Kind == kind_r2c_half || Kind == kind_c2r_half;
     static constexpr int NN = half ? 2 * NC : NC; // logical length (odd kinds: N = NC)
     // lane vectors of 16 bytes or more are stored as 16-byte chunks in NQ planes with an
@@ -124,6 +135,7 @@ template <class R, int Kind, int NC, int TT, int V, bool MI = false, bool PAIR =
     int pshift, padd;
     bool active;
     bool live = true;
+    bool active2 = false; // the second transform of a pair (two)
 
     __device__ __forceinline__ int sidx(int n) const { // LIN layout
         int i = sbase + n * p.Mb;
@@ -188,11 +200,34 @@ template <class R, int Kind, int NC, int TT, int V, bool MI = false, bool PAIR =
             ldv<V>(x + (2 * n + 1) * p.is1, b);
             sfor<0, V>([&](auto U) { o[U.value] = mk<R>(a[U.value], b[U.value]); });
         } else if constexpr (Kind == kind_r2c_full) {
-            R a[V];
+            R a[V], b[V];
             ldv<V>(static_cast<const R *>(p.in) + ib + n * p.is1, a);
-            sfor<0, V>([&](auto U) { o[U.value] = mk<R>(a[U.value], R(0)); });
+            sfor<0, V>([&](auto U) { b[U.value] = R(0); });
+            if constexpr (two) {
+                if (active2) {
+                    ldv<V>(static_cast<const R *>(p.in) + ib + p.is2 + n * p.is1, b);
+                }
+            }
+            sfor<0, V>([&](auto U) { o[U.value] = mk<R>(a[U.value], b[U.value]); });
         } else if constexpr (Kind == kind_c2r_full) {
-            const C *X = static_cast<const C *>(p.in) + ib;
+            c2r_full_load(static_cast<const C *>(p.in) + ib, n, o);
+            if constexpr (two) {
+                if (active2) {
+                    C b[V];
+                    c2r_full_load(static_cast<const C *>(p.in) + ib + p.is2, n, b);
+                    sfor<0, V>([&](auto U) {
+                        o[U.value] = mk<R>(o[U.value].x + b[U.value].y, o[U.value].y - b[U.value].x);
+                    });
+                }
+            }
+        } else {
+            c2r_half_load(n, o);
+        }
+    }
+
+    // c2r_full: the Hermitian extension of X[0..N/2] at n, conjugated for the forward engine
+    __device__ __forceinline__ void c2r_full_load(const C *X, int n, C *o) const {
+        if constexpr (Kind == kind_c2r_full) {
             if (2 * n <= NN) {
                 ldv<V>(X + n * p.is1, o);
                 sfor<0, V>([&](auto U) {
@@ -212,7 +247,11 @@ template <class R, int Kind, int NC, int TT, int V, bool MI = false, bool PAIR =
                     sfor<0, V>([&](auto U) { o[U.value] = adj_r2c_weight(o[U.value], NN - n); });
                 }
             }
-        } else {
+        }
+    }
+
+    __device__ __forceinline__ void c2r_half_load(int n, C *o) const {
+        if constexpr (Kind == kind_c2r_half) {
             // c2r_half: Z[n] = (x1 + x2) + (x1 - x2) i w_N^{+n}, x1 = X[n], x2 = conj X[NC-n]
             const C *X = static_cast<const C *>(p.in) + ib;
             C x1[V], x2[V];
@@ -262,6 +301,12 @@ template <class R, int Kind, int NC, int TT, int V, bool MI = false, bool PAIR =
             R a[V];
             sfor<0, V>([&](auto U) { a[U.value] = v[U.value].x; });
             stv<V>(static_cast<R *>(p.out) + ob + n * p.os1, a);
+            if constexpr (two) {
+                if (active2) {
+                    sfor<0, V>([&](auto U) { a[U.value] = -v[U.value].y; });
+                    stv<V>(static_cast<R *>(p.out) + ob + p.os2 + n * p.os1, a);
+                }
+            }
         } else if constexpr (Kind == kind_c2r_half) {
             R *x = static_cast<R *>(p.out) + ob;
             if (V == 1 && (p.flags & flag_vec_out)) {
@@ -620,9 +665,48 @@ __device__ __forceinline__ void ct_c2r_pre(const Ctx &c, int j) {
     }
 }
 
+// r2c (odd N) of a TWO tile: split Z (shared buffer) into the spectra of the pair's two
+// real transforms, X_k0[k] = (Z_k + conj Z_{N-k}) / 2, X_k0+1[k] = -i (Z_k - conj Z_{N-k}) / 2,
+// k = 0..(N-1)/2.
+template <class Ctx, class R, int NC, int TT, int V>
+__device__ __forceinline__ void ct_r2c_two_post(const Ctx &c, int j) {
+    using C = cplx<R>;
+    constexpr int cnt = NC / 2 + 1;
+    constexpr int ITERS = (cnt + TT - 1) / TT;
+    if constexpr (Ctx::may_idle) {
+        if (!c.live) {
+            return;
+        }
+    }
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int k = j + it * TT;
+        if ((cnt % TT == 0 || k < cnt) && c.active) {
+            C zk[V], zn[V], x0[V], x1[V];
+            c.sload(k, zk);
+            c.sload(k == 0 ? 0 : NC - k, zn);
+            sfor<0, V>([&](auto U) {
+                const C a = zk[U.value], b = zn[U.value];
+                C v = mk<R>((a.x + b.x) * R(0.5), (a.y - b.y) * R(0.5));
+                if (c.p.flags & flag_adj_c2r) {
+                    v = c.adj_c2r_weight(v, k, R(0));
+                }
+                x0[U.value] = v;
+                x1[U.value] = mk<R>((a.y + b.y) * R(0.5), (b.x - a.x) * R(0.5));
+            });
+            C *X = static_cast<C *>(c.p.out) + c.ob + k * c.p.os1;
+            stv<V>(X, x0);
+            if (c.active2) {
+                stv<V>(X + c.p.os2, x1);
+            }
+        }
+    }
+}
+
 template <class Ctx, class R, int NC, int TT, int V, int S, int L, int NS, int P, int... Rest>
 __device__ __forceinline__ void ct_run(const Ctx &c, int j) {
-    constexpr bool post = Ctx::kind_v == kind_r2c_half;
+    constexpr bool two_post = Ctx::two && Ctx::kind_v == kind_r2c_full;
+    constexpr bool post = Ctx::kind_v == kind_r2c_half || two_post;
     // c2r (even N), paired variant: the pre-process fills the shared buffer and the first
     // stage reads it; otherwise the first stage forms Z[n] in its own loads
     constexpr bool pre = S == 0 && Ctx::kind_v == kind_c2r_half && Ctx::paired_c2r;
@@ -638,6 +722,8 @@ __device__ __forceinline__ void ct_run(const Ctx &c, int j) {
     }
     if constexpr (sizeof...(Rest) > 0) {
         ct_run<Ctx, R, NC, TT, V, S + 1, L, NS * P, Rest...>(c, j);
+    } else if constexpr (two_post) {
+        ct_r2c_two_post<Ctx, R, NC, TT, V>(c, j);
     } else if constexpr (post) {
         ct_r2c_post<Ctx, R, NC, TT, V>(c, j);
     }
@@ -664,11 +750,12 @@ __device__ __forceinline__ void fft_tile_ct(const fft_params &p) {
 }
 
 // The same tile for the persistent ragged kernel: tile index given, block possibly larger
-// than the tile's (Mb / V) * TT * Kb threads.
-template <class R, int Kind, int NC, int TT, int V, int... Ps>
-__device__ __forceinline__ void fft_tile_ct_ragged(const fft_params &p, long long tile) {
+// than the tile's (Mb / V) * TT * Kb threads.  TWO: odd real N, the tile's k index counts
+// pairs of transforms when the plan sets flag_pair (ct_ctx::two).
+template <class R, int Kind, int NC, int TT, int V, bool TWO, int... Ps>
+__device__ __forceinline__ void fft_tile_ct_ragged_t(const fft_params &p, long long tile) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    using Ctx = ct_ctx<R, Kind, NC, TT, V, true>;
+    using Ctx = ct_ctx<R, Kind, NC, TT, V, true, false, TWO>;
     const int tid = threadIdx.x;
     const int mvb = p.Mb / V;
     const bool live = tid < mvb * TT * p.Kb;
@@ -679,11 +766,24 @@ __device__ __forceinline__ void fft_tile_ct_ragged(const fft_params &p, long lon
     const long long kt = tile / p.m_tiles;
     const int m_l = mv * V;
     const long long m = mt * p.Mb + m_l;
-    const long long k = kt * p.Kb + k_l;
+    long long k = kt * p.Kb + k_l;
+    bool pair = false;
+    if constexpr (Ctx::two) {
+        pair = (p.flags & flag_pair) != 0;
+        if (pair) {
+            k *= 2;
+        }
+    }
     const int sbase = Ctx::LIN ? k_l * NC * p.Mb + m_l : k_l * NC * mvb + mv;
     Ctx c{p, reinterpret_cast<cplx<R> *>(smem_raw), m + k * p.is2, m + k * p.os2, sbase,
           p.pad_shift, p.pad_add, live && (m < p.M) && (k < p.K), live};
+    c.active2 = pair && c.active && k + 1 < p.K;
     ct_run<Ctx, R, NC, TT, V, 0, sizeof...(Ps), 1, Ps...>(c, j);
+}
+
+template <class R, int Kind, int NC, int TT, int V, int... Ps>
+__device__ __forceinline__ void fft_tile_ct_ragged(const fft_params &p, long long tile) {
+    fft_tile_ct_ragged_t<R, Kind, NC, TT, V, false, Ps...>(p, tile);
 }
 
 // Ragged batches, one CTA per unit: stage the unit's parameters (item un.x, tile un.y)

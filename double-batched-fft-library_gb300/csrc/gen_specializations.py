@@ -254,9 +254,12 @@ def cover_units(outdir):
                '#include "engine_ct.cuh"', '#include "kernels.hpp"', '', 'namespace gbfft {', '']
         for i in idx:
             prec, kind, nc, T, rad, V = ents[i]
-            targs = 'float, %d, %d, %d, %d, %s' % (kind, nc, T, V, ', '.join(map(str, rad)))
+            # odd real N (kinds 2, 4): tiles that run two real transforms per complex FFT
+            # when the plan sets flag_pair
+            two = 'true' if kind in (2, 4) else 'false'
+            targs = 'float, %d, %d, %d, %d, %s, %s' % (kind, nc, T, V, two, ', '.join(map(str, rad)))
             src += ['__global__ void __launch_bounds__(256, %d) cover_ct_%d(const __grid_constant__ fft_params p) {' % (tile_min_blocks(rad), i),
-                    '    fft_tile_ct_ragged<%s>(p, blockIdx.x);' % targs, '}', '']
+                    '    fft_tile_ct_ragged_t<%s>(p, blockIdx.x);' % targs, '}', '']
         src += ['const void *cover_ct_kernel_%d(int i) {' % g, '    switch (i) {']
         for i in idx:
             src += ['    case %d:' % i, '        return reinterpret_cast<const void *>(&cover_ct_%d);' % i]

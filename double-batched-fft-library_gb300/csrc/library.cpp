@@ -1262,6 +1262,14 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
             }
         }
     }
+    // odd real N on a compile-time cover tile: the transforms k and k + 1 share one complex
+    // FFT (not for the adjoint forms, whose Hermitian weights the pairing does not apply)
+    bool const pair = cover_id >= 0 && (ps.kind == kind_r2c_full || ps.kind == kind_c2r_full) &&
+                      K >= 2 && (flags & (flag_adj_r2c | flag_adj_c2r)) == 0;
+    if (pair) {
+        flags |= flag_pair;
+    }
+    long long const Kt = pair ? (K + 1) / 2 : K; // transforms along K of the tiles
     int const max_block = q.max_block > 0 ? q.max_block : (ct ? 256 : 512);
     // the runtime kernel ping-pongs between two buffers when a stage goes shared->shared;
     // compile-time kernels run their stages in place in one buffer
@@ -1307,7 +1315,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         return last + (last >> 2) + 1;
     };
     int Kb = reqKb > 0 ? reqKb : std::max(1, std::min(256, max_block) / lanes_per_k);
-    Kb = static_cast<int>(std::min<long long>(Kb, K));
+    Kb = static_cast<int>(std::min<long long>(Kb, Kt));
     Kb = std::max(Kb, 1);
     while (Kb * lanes_per_k > max_block && Kb > 1) {
         Kb /= 2;
@@ -1361,7 +1369,7 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     if (ps.kind == kind_c2r_half && q.os1 == 1 && M == 1 && q.os2 % 2 == 0) {
         p.flags |= flag_vec_out;
     }
-    long long k_tiles = (K + Kb - 1) / Kb;
+    long long k_tiles = (Kt + Kb - 1) / Kb;
     if (static_cast<long long>(p.m_tiles) * k_tiles > 0x7fffffffLL) {
         bad_config("tensor too large for one launch");
     }
@@ -1384,8 +1392,8 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     for (int s = 0; s < L; ++s) {
         id << (s ? "x" : "") << rad[s];
     }
-    id << "_T" << T << "_V" << V << "_Kb" << Kb << "_is" << q.is1 << "_" << q.is2 << "_os" << q.os1 << "_"
-       << q.os2;
+    id << "_T" << T << "_V" << V << "_Kb" << Kb << (pair ? "_pair" : "") << "_is" << q.is1 << "_"
+       << q.is2 << "_os" << q.os1 << "_" << q.os2;
     if (q.load_fn && *q.load_fn) {
         id << "_" << q.load_fn;
     }

@@ -27,6 +27,7 @@ constexpr int flag_adj_c2r = 8;   // adjoint of c2r, run as a r2c kernel (Hermit
 constexpr int flag_scale_out = 16; // multiply the output by params.scale
 constexpr int flag_vec_in = 32;   // real input pairs x[2n], x[2n+1] are adjacent and aligned
 constexpr int flag_vec_out = 64;  // real output pairs are adjacent and aligned
+constexpr int flag_pair = 128;    // odd real N: the transforms k and k + 1 share one complex FFT
 
 struct fft_params {
     const void *in;

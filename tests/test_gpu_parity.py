@@ -190,7 +190,8 @@ def test_c2r_nd(bb, po, torch_cuda, prec, Ns, inplace):
 
 @pytest.mark.parametrize('prec', PRECS)
 @pytest.mark.parametrize('Ns,K,M,inplace', [((8,), 16, 1, True), ((64,), 16, 8, True),
-                                             ((212,), 16, 8, True), ((8,), 16, 1, False),
+                                             ((212,), 16, 8, True), ((135,), 7, 8, True),
+                                             ((509,), 5, 4, True), ((8,), 16, 1, False),
                                              ((64,), 16, 8, False), ((212,), 16, 1, False),
                                              ((8, 8, 8), 11, 7, True), ((96, 96, 80), 1, 1, True)])
 def test_real_identity(bb, po, torch_cuda, prec, Ns, K, M, inplace):
@@ -362,6 +363,38 @@ def test_prime_factor_lengths(bb, po, torch_cuda, type):
         e = rel_l2(out, ref)
         worst = max(worst, e)
         assert e <= TOL[4], (N, M, K, d, e)
+    print('worst rel-L2', worst)
+
+
+# every odd length 17..511 with prime factors <= 61 (compile-time tiles that run two real
+# transforms along K per complex FFT)
+ODD_REAL_N = [n for n in range(17, 512, 2) if _largest_prime_factor(n) <= 61]
+
+
+@pytest.mark.parametrize('type', [1, 2])
+def test_odd_real_lengths_paired(bb, po, torch_cuda, type):
+    """Float r2c / c2r of every odd N <= 511 with prime factors <= 61, random double
+    batching with odd and even K (the last pair of an odd K has one transform), against
+    the oracle in FP64 within the float tolerance."""
+    torch = torch_cuda
+    rng = np.random.default_rng(31 + type)
+    worst = 0.0
+    for N in ODD_REAL_N:
+        M = int(rng.choice([1, 2, 3, 8]))
+        K = int(rng.integers(1, 10))
+        d = bb.BACKWARD if type == 2 else bb.FORWARD
+        cfg = bb.configuration(1, [M, N, K], precision=bb.F32, type=type, direction=d)
+        nin = N // 2 + 1 if type == 2 else N
+        nout = N // 2 + 1 if type == 1 else N
+        if type == 1:
+            x = rng.standard_normal(M * nin * K).astype(np.float32)
+        else:
+            x = (rng.standard_normal(M * nin * K) + 1j * rng.standard_normal(M * nin * K)).astype(np.complex64)
+        out = run(bb, torch, cfg, x, M * nout * K, np.float32 if type == 2 else np.complex64)
+        ref = po.oracle_fft(1, [M, N, K], type, d, x.astype(np.complex128 if type != 1 else np.float64), prec=8)
+        e = rel_l2(out, ref)
+        worst = max(worst, e)
+        assert e <= TOL[4], (N, M, K, e)
     print('worst rel-L2', worst)
 
 
