@@ -645,10 +645,22 @@ def leg_c2c_cfg1(bb, torch, stream, hbm_peak, steps, warmup):
         g.replay()
     msg = event_time(torch, torch.cuda.current_stream(), g.replay, max(steps, 4)) / nb
     best = min(ms, msg)
+    # the floor at this size: a device copy of the same 8 MiB per launch (same bytes read
+    # and written), 24 rotating buffer pairs in one graph
+    gc = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(gc, stream=cs):
+        for i in range(nb):
+            ys[i].copy_(xs[i])
+    stream.wait_stream(cs)
+    for _ in range(warmup):
+        gc.replay()
+    msc = event_time(torch, torch.cuda.current_stream(), gc.replay, max(steps, 4)) / nb
     return {'value': round(b / best / 1e6, 1), 'unit': 'GB/s',
             'frac_of_hbm': round(b / best / 1e6 / hbm_peak, 3),
             'us_per_launch_stream': round(ms * 1e3, 2), 'us_per_launch_graph': round(msg * 1e3, 2),
             'gbs_stream': round(b / ms / 1e6, 1), 'gbs_graph': round(b / msg / 1e6, 1),
+            'copy_us_per_launch_graph': round(msc * 1e3, 2), 'copy_gbs_graph': round(b / msc / 1e6, 1),
+            'frac_of_copy_at_this_size': round(msc / best, 3),
             'l2': '24 rotating buffer pairs, 384 MiB'}
 
 

@@ -48,16 +48,40 @@ __host__ __device__ constexpr int tw_offset(int L, int s) {
     return s <= 1 ? 0 : tw_offset(L, s - 1) + (radix_of(L, s - 1) - 1) * span_of(L, s - 1);
 }
 __host__ __device__ constexpr int tw_entries(int L) { return tw_offset(L, stages_of(L)); }
+// spare shared elements after every 16 (chosen with a model of the 32 banks, 8-byte
+// elements in half-warp phases, over every shared access of the tile)
+__host__ __device__ constexpr int pad_of(int L, int MB) { return L == 512 && MB % 2 == 0 ? 2 : 1; }
+
+// Shared index of element i of the tile buffer (MB transforms along M interleaved): PAD
+// spare elements after every 16.
+template <int PAD> __device__ __forceinline__ int padded(int i) { return i + (i >> 4) * PAD; }
+
+// Shared indices of the elements n0 + r * STEP (r = 0, 1, ...) of a transform whose
+// element 0 sits at `base`: when STEP * MB is a multiple of 16 the padding is linear in r
+// and the index is a compile-time offset from the first one.
+template <int MB, int PAD, int STEP> struct sm_run {
+    int a0, i0;
+    __device__ __forceinline__ sm_run(int base, int n0) : i0(base + n0 * MB) { a0 = padded<PAD>(i0); }
+    __device__ __forceinline__ int at(int r) const {
+        if constexpr ((STEP * MB) % 16 == 0) {
+            return a0 + r * (STEP * MB / 16) * (16 + PAD);
+        } else {
+            return padded<PAD>(i0 + r * STEP * MB);
+        }
+    }
+};
 
 // One radix-R Stockham stage of the length-L transform on T threads per transform, the
 // earlier stages spanning Ns: butterfly b reads elements b + r L / R (times the twiddles
 // w_L^{-r (b mod Ns) L / (Ns R)} = tw[(r - 1) Ns + b mod Ns]) and writes
-// (b / Ns) Ns R + (b mod Ns) + r Ns.  `load(n)` / `store(n, v)` move element n; `HALF_IN`:
-// inputs at r >= R / 2 are zero; `HALF_OUT`: outputs at r >= R / 2 are not needed; `MID`:
-// barrier between the loads and the stores (in-place shared-memory stage).  Threads
-// beyond the tile hold j = 1 << 20.
-template <int L, int T, int R, int Ns, bool HALF_IN, bool HALF_OUT, bool MID, class Load, class Store>
-__device__ __forceinline__ void stage(int j, const float2 *tw, Load load, Store store) {
+// (b / Ns) Ns R + (b mod Ns) + r Ns.  `load(n, a)` / `store(n, a, v)` move element n, a its
+// shared index (SRC_SM / DST_SM: the stage reads / writes the tile buffer sm itself);
+// `HALF_IN`: inputs at r >= R / 2 are zero; `HALF_OUT`: outputs at r >= R / 2 are not
+// needed; `MID`: barrier between the loads and the stores (in-place shared-memory stage).
+// Threads beyond the tile hold j = 1 << 20.
+template <int L, int T, int MB, int PAD, int R, int Ns, bool HALF_IN, bool HALF_OUT, bool MID,
+          class Load, class Store>
+__device__ __forceinline__ void stage(int j, int base, const float2 *tw, Load load, Store store) {
     constexpr int nb = L / R;
     constexpr int IT = (nb + T - 1) / T;
     float2 v[IT][R];
@@ -66,11 +90,12 @@ __device__ __forceinline__ void stage(int j, const float2 *tw, Load load, Store 
         const int b = j + it * T;
         if (b < nb) {
             const int kk = b % Ns;
+            const sm_run<MB, PAD, nb> in(base, b);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 float2 x = make_float2(0.f, 0.f);
                 if (!HALF_IN || r < R / 2) {
-                    x = load(b + r * nb);
+                    x = load(b + r * nb, in.at(r));
                     if (Ns > 1 && r > 0) {
                         x = cmul(x, tw[(r - 1) * Ns + kk]);
                     }
@@ -88,22 +113,23 @@ __device__ __forceinline__ void stage(int j, const float2 *tw, Load load, Store 
         const int b = j + it * T;
         if (b < nb) {
             const int o = (b / Ns) * Ns * R + b % Ns;
+            const sm_run<MB, PAD, Ns> out(base, o);
 #pragma unroll
             for (int r = 0; r < (HALF_OUT ? R / 2 : R); ++r) {
-                store(o + r * Ns, v[it][r]);
+                store(o + r * Ns, out.at(r), v[it][r]);
             }
         }
     }
 }
 
 // Middle stages s = 1 .. S - 2 of a transform, shared memory to shared memory.
-template <int L, int s, class SmLoad, class SmStore>
-__device__ __forceinline__ void middle(int j, const float2 *tw, SmLoad ld, SmStore st) {
+template <int L, int MB, int PAD, int s, class SmLoad, class SmStore>
+__device__ __forceinline__ void middle(int j, int base, const float2 *tw, SmLoad ld, SmStore st) {
     if constexpr (s < stages_of(L) - 1) {
-        stage<L, threads_of(L), radix_of(L, s), span_of(L, s), false, false, true>(
-            j, tw + tw_offset(L, s), ld, st);
+        stage<L, threads_of(L), MB, PAD, radix_of(L, s), span_of(L, s), false, false, true>(
+            j, base, tw + tw_offset(L, s), ld, st);
         __syncthreads();
-        middle<L, s + 1>(j, tw, ld, st);
+        middle<L, MB, PAD, s + 1>(j, base, tw, ld, st);
     }
 }
 
@@ -111,23 +137,26 @@ __device__ __forceinline__ void middle(int j, const float2 *tw, SmLoad ld, SmSto
 // k0 = 2k and k0 + 1 of the tile's pair index k.  r2c: z = x_k0 + i x_k0+1, and with
 // Z = FFT(z), X_k0[k] = (Z_k + conj Z_{N-k}) / 2, X_k0+1[k] = -i (Z_k - conj Z_{N-k}) / 2.
 // c2r: the engine's load gives A = conj X_k0 and B = conj X_k0+1 (Hermitian extensions),
-// the forward transform of A - i B is x_k0 - i x_k0+1.
-template <int Kind, int L, bool PAIR>
+// the forward transform of A - i B is x_k0 - i x_k0+1.  MB: transforms along M per tile
+// (1, 2 or 4, compile-time so that the shared indices of a butterfly are constant
+// offsets of one another).
+template <int Kind, int L, bool PAIR, int MB>
 __device__ __forceinline__ void tile(const fft_params &p, long long t, const float2 *tw) {
     constexpr int T = threads_of(L);
     constexpr int S = stages_of(L);
     constexpr int R0 = radix_of(L, 0);
     constexpr int RL = radix_of(L, S - 1);
     constexpr int NL = span_of(L, S - 1);
+    constexpr int PAD = pad_of(L, MB);
     const float2 *twl = tw + tw_offset(L, S - 1); // last stage's twiddles
     extern __shared__ __align__(16) unsigned char smem_raw[];
     int j;
     auto c = make_ctx<float, Kind, default_io>(p, smem_raw, T, L, j, t);
     auto c2 = c; // the second transform of a pair
     if constexpr (PAIR) {
-        const int m_l = threadIdx.x % p.Mb;
-        const int k_l = threadIdx.x / (p.Mb * T);
-        const long long m = (t % p.m_tiles) * p.Mb + m_l;
+        const int m_l = threadIdx.x % MB;
+        const int k_l = threadIdx.x / (MB * T);
+        const long long m = (t % p.m_tiles) * MB + m_l;
         const long long k0 = 2 * ((t / p.m_tiles) * p.Kb + k_l);
         c.ib = m + k0 * p.is2;
         c.ob = m + k0 * p.os2;
@@ -137,12 +166,14 @@ __device__ __forceinline__ void tile(const fft_params &p, long long t, const flo
         c2.active = c.active && k0 + 1 < p.K;
     }
     const int Nc = p.Nc;
+    const int base = c.sbase;
+    float2 *sm = c.sm;
     const float2 *chirp = static_cast<const float2 *>(p.bs);
     const float2 *bhat = chirp + Nc;
-    auto sm_load = [&](int n) { return c.sm[c.sidx(0, n)]; };
-    auto sm_store = [&](int n, float2 v) { c.sm[c.sidx(0, n)] = v; };
+    auto sm_load = [&](int, int a) { return sm[a]; };
+    auto sm_store = [&](int, int a, float2 v) { sm[a] = v; };
     // forward transform of a = x . chirp: first stage from global memory
-    auto g_load = [&](int n) {
+    auto g_load = [&](int n, int) {
         float2 v = make_float2(0.f, 0.f);
         if (n < Nc && c.active) {
             v = c.template gload<0>(n);
@@ -154,36 +185,36 @@ __device__ __forceinline__ void tile(const fft_params &p, long long t, const flo
         }
         return v;
     };
-    stage<L, T, R0, 1, true, false, false>(j, tw, g_load, sm_store);
+    stage<L, T, MB, PAD, R0, 1, true, false, false>(j, base, tw, g_load, sm_store);
     __syncthreads();
-    middle<L, 1>(j, tw, sm_load, sm_store);
+    middle<L, MB, PAD, 1>(j, base, tw, sm_load, sm_store);
     // last forward stage: times FFT(b) / L, conjugated for the inverse transform
-    auto mul_store = [&](int n, float2 v) {
+    auto mul_store = [&](int n, int a, float2 v) {
         v = cmul(v, __ldg(bhat + n));
-        c.sm[c.sidx(0, n)] = make_float2(v.x, -v.y);
+        sm[a] = make_float2(v.x, -v.y);
     };
-    stage<L, T, RL, NL, false, false, true>(j, twl, sm_load, mul_store);
+    stage<L, T, MB, PAD, RL, NL, false, false, true>(j, base, twl, sm_load, mul_store);
     __syncthreads();
     // inverse transform (of the conjugate)
-    stage<L, T, R0, 1, false, false, true>(j, tw, sm_load, sm_store);
+    stage<L, T, MB, PAD, R0, 1, false, false, true>(j, base, tw, sm_load, sm_store);
     __syncthreads();
-    middle<L, 1>(j, tw, sm_load, sm_store);
+    middle<L, MB, PAD, 1>(j, base, tw, sm_load, sm_store);
     if constexpr (Kind == kind_r2c_half || (PAIR && Kind == kind_r2c_full)) {
         // Z_k = c_k conj(y_k) into shared memory, then the r2c post-process
-        auto z_store = [&](int k, float2 y) {
+        auto z_store = [&](int k, int a, float2 y) {
             if (k < Nc) {
-                c.sm[c.sidx(0, k)] = cmul(make_float2(y.x, -y.y), __ldg(chirp + k));
+                sm[a] = cmul(make_float2(y.x, -y.y), __ldg(chirp + k));
             }
         };
-        stage<L, T, RL, NL, false, true, true>(j, twl, sm_load, z_store);
+        stage<L, T, MB, PAD, RL, NL, false, true, true>(j, base, twl, sm_load, z_store);
         __syncthreads();
         if constexpr (Kind == kind_r2c_half) {
             r2c_post<0, T>(c, j, 0);
         } else if (c.active) {
             // split the spectra of the two real transforms
             for (int k = j; 2 * k <= Nc; k += T) {
-                const float2 zk = c.sm[c.sidx(0, k)];
-                const float2 zn = c.sm[c.sidx(0, k == 0 ? 0 : Nc - k)];
+                const float2 zk = sm[padded<PAD>(base + k * MB)];
+                const float2 zn = sm[padded<PAD>(base + (k == 0 ? 0 : Nc - k) * MB)];
                 c.template gstore<0>(k, make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y)));
                 if (c2.active) {
                     c2.template gstore<0>(k, make_float2(0.5f * (zk.y + zn.y), 0.5f * (zn.x - zk.x)));
@@ -191,7 +222,7 @@ __device__ __forceinline__ void tile(const fft_params &p, long long t, const flo
             }
         }
     } else {
-        auto g_store = [&](int k, float2 y) {
+        auto g_store = [&](int k, int, float2 y) {
             if (k < Nc && c.active) {
                 const float2 v = cmul(make_float2(y.x, -y.y), __ldg(chirp + k));
                 c.template gstore<0>(k, v);
@@ -202,12 +233,12 @@ __device__ __forceinline__ void tile(const fft_params &p, long long t, const flo
                 }
             }
         };
-        stage<L, T, RL, NL, false, true, false>(j, twl, sm_load, g_store);
+        stage<L, T, MB, PAD, RL, NL, false, true, false>(j, base, twl, sm_load, g_store);
     }
 }
 
 // One tile per CTA; the stage twiddles are copied into shared memory after the tile buffer
-template <int Kind, int L, bool PAIR> __device__ __forceinline__ void tiles(const fft_params &p) {
+template <int Kind, int L, bool PAIR, int MB> __device__ __forceinline__ void tiles(const fft_params &p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *tw = reinterpret_cast<float2 *>(smem_raw) + p.buf_elems;
     const float2 *gtw = static_cast<const float2 *>(p.bs) + p.Nc + L;
@@ -215,22 +246,34 @@ template <int Kind, int L, bool PAIR> __device__ __forceinline__ void tiles(cons
         tw[i] = __ldg(gtw + i);
     }
     __syncthreads();
-    tile<Kind, L, PAIR>(p, blockIdx.x, tw);
+    tile<Kind, L, PAIR, MB>(p, blockIdx.x, tw);
 }
 
-template <int Kind, bool PAIR>
+template <int Kind, bool PAIR, int MB>
 __global__ void __launch_bounds__(256, 4) bluestein_kernel(const __grid_constant__ fft_params p) {
     switch (p.bL) {
     case 256:
-        tiles<Kind, 256, PAIR>(p);
+        tiles<Kind, 256, PAIR, MB>(p);
         break;
     case 512:
-        tiles<Kind, 512, PAIR>(p);
+        tiles<Kind, 512, PAIR, MB>(p);
         break;
     case 1024:
-        tiles<Kind, 1024, PAIR>(p);
+        tiles<Kind, 1024, PAIR, MB>(p);
         break;
     }
+}
+
+template <int Kind, bool PAIR> const void *kernel_mb(int mb) {
+    switch (mb) {
+    case 1:
+        return reinterpret_cast<const void *>(&bluestein_kernel<Kind, PAIR, 1>);
+    case 2:
+        return reinterpret_cast<const void *>(&bluestein_kernel<Kind, PAIR, 2>);
+    case 4:
+        return reinterpret_cast<const void *>(&bluestein_kernel<Kind, PAIR, 4>);
+    }
+    return nullptr;
 }
 
 } // namespace blu
@@ -239,20 +282,20 @@ int bluestein_threads(int L) { return blu::threads_of(L); }
 int bluestein_stages(int L) { return blu::stages_of(L); }
 int bluestein_radix(int L, int s) { return blu::radix_of(L, s); }
 
-const void *bluestein_kernel(int kind, bool pair) {
+int bluestein_pad(int L, int mb) { return blu::pad_of(L, mb); }
+
+const void *bluestein_kernel(int kind, bool pair, int mb) {
     switch (kind) {
     case kind_c2c:
-        return reinterpret_cast<const void *>(&blu::bluestein_kernel<kind_c2c, false>);
+        return blu::kernel_mb<kind_c2c, false>(mb);
     case kind_r2c_half:
-        return reinterpret_cast<const void *>(&blu::bluestein_kernel<kind_r2c_half, false>);
+        return blu::kernel_mb<kind_r2c_half, false>(mb);
     case kind_r2c_full:
-        return pair ? reinterpret_cast<const void *>(&blu::bluestein_kernel<kind_r2c_full, true>)
-                    : reinterpret_cast<const void *>(&blu::bluestein_kernel<kind_r2c_full, false>);
+        return pair ? blu::kernel_mb<kind_r2c_full, true>(mb) : blu::kernel_mb<kind_r2c_full, false>(mb);
     case kind_c2r_half:
-        return reinterpret_cast<const void *>(&blu::bluestein_kernel<kind_c2r_half, false>);
+        return blu::kernel_mb<kind_c2r_half, false>(mb);
     case kind_c2r_full:
-        return pair ? reinterpret_cast<const void *>(&blu::bluestein_kernel<kind_c2r_full, true>)
-                    : reinterpret_cast<const void *>(&blu::bluestein_kernel<kind_c2r_full, false>);
+        return pair ? blu::kernel_mb<kind_c2r_full, true>(mb) : blu::kernel_mb<kind_c2r_full, false>(mb);
     }
     return nullptr;
 }

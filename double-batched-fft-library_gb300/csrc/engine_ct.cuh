@@ -103,7 +103,7 @@ template <int V> __device__ __forceinline__ void stv(double *p, const double *o)
 }
 
 template <class R, int Kind, int NC, int TT, int V, bool MI = false, bool PAIR = false,
-          bool TWO = false>
+          bool TWO = false, bool REGP = false>
 struct ct_ctx {
     using C = cplx<R>;
     static constexpr int kind_v = Kind;
@@ -121,6 +121,9 @@ struct ct_ctx {
     // Without the flag a TWO tile runs single transforms (r2c still through the
     // post-process, which then returns Z_k).
     static constexpr bool two = TWO && (Kind == kind_r2c_full || Kind == kind_c2r_full);
+    // the prime radix 17..47 of a short length runs in registers, one butterfly per thread
+    // (the generic stage with dft<P>), instead of the tensor-core / shared-memory form
+    static constexpr bool reg_prime = REGP;
     static constexpr bool half = Kind == kind_r2c_half || Kind == kind_c2r_half;
     static constexpr int NN = half ? 2 * NC : NC; // logical length (odd kinds: N = NC)
     // lane vectors of 16 bytes or more are stored as 16-byte chunks in NQ planes with an
@@ -487,7 +490,7 @@ __device__ __forceinline__ void ct_stage_prime(const Ctx &c, int j) {
 // One in-place Stockham stage with compile-time sizes (see engine.cuh for the formulas).
 template <int P, int NS, bool SRC_G, bool DST_G, class Ctx, class R, int NC, int TT, int V>
 __device__ __forceinline__ void ct_stage(const Ctx &c, int j) {
-    if constexpr (ct_big_prime(P)) {
+    if constexpr (ct_big_prime(P) && !Ctx::reg_prime) {
         static_assert(!SRC_G && !DST_G && V == 1, "prime stages run shared to shared, V = 1");
         ct_stage_prime<P, NS, Ctx, R, NC, TT>(c, j);
         return;
@@ -751,11 +754,12 @@ __device__ __forceinline__ void fft_tile_ct(const fft_params &p) {
 
 // The same tile for the persistent ragged kernel: tile index given, block possibly larger
 // than the tile's (Mb / V) * TT * Kb threads.  TWO: odd real N, the tile's k index counts
-// pairs of transforms when the plan sets flag_pair (ct_ctx::two).
-template <class R, int Kind, int NC, int TT, int V, bool TWO, int... Ps>
+// pairs of transforms when the plan sets flag_pair (ct_ctx::two); REGP: the prime stage
+// runs in registers (ct_ctx::reg_prime).
+template <class R, int Kind, int NC, int TT, int V, bool TWO, bool REGP, int... Ps>
 __device__ __forceinline__ void fft_tile_ct_ragged_t(const fft_params &p, long long tile) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    using Ctx = ct_ctx<R, Kind, NC, TT, V, true, false, TWO>;
+    using Ctx = ct_ctx<R, Kind, NC, TT, V, true, false, TWO, REGP>;
     const int tid = threadIdx.x;
     const int mvb = p.Mb / V;
     const bool live = tid < mvb * TT * p.Kb;
@@ -783,7 +787,7 @@ __device__ __forceinline__ void fft_tile_ct_ragged_t(const fft_params &p, long l
 
 template <class R, int Kind, int NC, int TT, int V, int... Ps>
 __device__ __forceinline__ void fft_tile_ct_ragged(const fft_params &p, long long tile) {
-    fft_tile_ct_ragged_t<R, Kind, NC, TT, V, false, Ps...>(p, tile);
+    fft_tile_ct_ragged_t<R, Kind, NC, TT, V, false, false, Ps...>(p, tile);
 }
 
 // Ragged batches, one CTA per unit: stage the unit's parameters (item un.x, tile un.y)

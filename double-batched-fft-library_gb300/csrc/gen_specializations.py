@@ -77,7 +77,21 @@ def choose_radices(nc):
 BIG_PRIMES = {17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61}
 
 
-def tile_threads(nc, rad, V=1):
+# A prime complex length 17..47 (c2c N = P, real N = 2P or odd N = P) runs its one
+# radix-P butterfly per transform in registers on one thread (dft<P> with literal
+# coefficients), without the copy stages around it: the tensor-core form needs shared
+# memory on both sides and several butterflies per warp, which such lengths do not have.
+# (Measured: with two or more butterflies per transform, 2P or 4P, the tensor-core form
+# stayed faster.)
+REG_PRIME_MAX = 47
+
+
+def reg_prime_length(nc):
+    """Same rule as reg_prime_length() in library.cpp."""
+    return nc in BIG_PRIMES and nc <= REG_PRIME_MAX
+
+
+def tile_threads(nc, rad, V=1, reg=False):
     """Threads per transform of a compile-time tile (same rule as tile_threads() in
     library.cpp): the count that leaves the fewest thread slots idle over the stages
     (a stage of nb butterflies runs ceil(nb / T) rounds on T threads), with at most 32
@@ -86,15 +100,19 @@ def tile_threads(nc, rad, V=1):
     transform: 32-byte sectors when M = 1); ties go to more threads.  The tensor-core
     prime stages use every warp of the block and do not count, but with one of them T is
     at most 4 x its butterflies per transform where possible, so that a block of 256
-    threads holds at least 64 of its butterflies (8 per warp)."""
-    nbmax = max([nc // r for r in rad if r not in BIG_PRIMES] + [1])
-    tcap = min([4 * (nc // r) for r in rad if r in BIG_PRIMES] + [256])
+    threads holds at least 64 of its butterflies (8 per warp).  `reg`: the prime length runs
+    in registers on one thread per transform (reg_prime_length)."""
+    if reg:
+        return 1
+    tc = BIG_PRIMES
+    nbmax = max([nc // r for r in rad if r not in tc] + [1])
+    tcap = min([4 * (nc // r) for r in rad if r in tc] + [256])
     for hi in (min(nc, 256, tcap), min(nc, 256)):
         best_t, best_cost = None, None
         for t in range(min(4, nbmax), hi + 1):
             cost, ok = 0, True
             for r in rad:
-                if r in BIG_PRIMES:
+                if r in tc:
                     continue
                 rounds = -(-(nc // r) // t)
                 if rounds * r * V > 32:
@@ -108,21 +126,23 @@ def tile_threads(nc, rad, V=1):
     return 1
 
 
-def stage_list(nc, kind, ragged=False):
+def stage_list(nc, kind, ragged=False, reg_ok=False):
     """Radices incl. the copy stages the host adds, and threads per transform (the rules
     of make_1d_pass in library.cpp; `ragged`: a compile-time tile, i.e. a pass of a ragged
-    batch or a plan on a tile kernel)."""
+    batch or a plan on a tile kernel; `reg_ok`: a cover tile, whose prime stage may run in
+    registers)."""
     rad = choose_radices(nc)
-    if rad[0] not in UNROLLED:
+    reg = ragged and reg_ok and reg_prime_length(nc)
+    if rad[0] not in UNROLLED and not reg:
         rad = [1] + rad
     real = kind != 0
     post = kind == 1
-    if not post and rad[-1] in BIG_PRIMES:
+    if not post and rad[-1] in BIG_PRIMES and not reg:
         rad = rad + [1]
     if real and not post and len(rad) == 1:
         rad = rad + [1]
     if ragged:
-        return rad, tile_threads(nc, rad)
+        return rad, tile_threads(nc, rad, reg=reg)
     pu = max([r for r in rad if r in UNROLLED] + [1])
     T = max(1, nc // pu) if pu > 1 else min(nc, 64)
     ptg = max([r for r in rad if r in BIG_PRIMES] + [0])
@@ -211,11 +231,18 @@ def ragged_entries():
     return out
 
 
-def tile_min_blocks(rad):
+def reg_prime_tile(nc, rad):
+    """A cover tile whose prime stage runs in registers (stage_list with reg_ok): the
+    prime is its last radix and no copy stage precedes it."""
+    return reg_prime_length(nc) and rad[0] != 1 and any(r in BIG_PRIMES for r in rad)
+
+
+def tile_min_blocks(rad, reg=False):
     """Resident 256-thread CTAs the register budget of a tile kernel is sized for: 3 (80
     registers) with a tensor-core prime stage, whose tiles are otherwise limited by the
-    latency of 2 CTAs per SM at 128 registers; 2 for the others."""
-    return 3 if any(r in BIG_PRIMES for r in rad) else 2
+    latency of 2 CTAs per SM at 128 registers; 2 for the others (and for a prime stage in
+    registers, which holds up to 47 complex values per thread)."""
+    return 3 if any(r in BIG_PRIMES for r in rad) and not reg else 2
 
 
 def largest_prime_factor(n):
@@ -235,7 +262,7 @@ def cover_entries():
         for nc in ncs:
             if largest_prime_factor(nc) > 61 or (kind, nc) in plan or (kind, nc) in rag:
                 continue
-            rad, T = stage_list(nc, kind, ragged=True)
+            rad, T = stage_list(nc, kind, ragged=True, reg_ok=True)
             out.append((4, kind, nc, T, rad, 1))
     return out
 
@@ -257,8 +284,10 @@ def cover_units(outdir):
             # odd real N (kinds 2, 4): tiles that run two real transforms per complex FFT
             # when the plan sets flag_pair
             two = 'true' if kind in (2, 4) else 'false'
-            targs = 'float, %d, %d, %d, %d, %s, %s' % (kind, nc, T, V, two, ', '.join(map(str, rad)))
-            src += ['__global__ void __launch_bounds__(256, %d) cover_ct_%d(const __grid_constant__ fft_params p) {' % (tile_min_blocks(rad), i),
+            reg = reg_prime_tile(nc, rad)
+            targs = 'float, %d, %d, %d, %d, %s, %s, %s' % (kind, nc, T, V, two, 'true' if reg else 'false',
+                                                       ', '.join(map(str, rad)))
+            src += ['__global__ void __launch_bounds__(256, %d) cover_ct_%d(const __grid_constant__ fft_params p) {' % (tile_min_blocks(rad, reg), i),
                     '    fft_tile_ct_ragged_t<%s>(p, blockIdx.x);' % targs, '}', '']
         src += ['const void *cover_ct_kernel_%d(int i) {' % g, '    switch (i) {']
         for i in idx:

@@ -33,8 +33,10 @@ int cover_ct_lookup(int prec, int kind, int nc, int T, const int *rad, int L);
 const void *cover_ct_kernel(int i);
 
 // Bluestein's algorithm for float lengths with a prime factor above 61 (bluestein.cu)
-// pair: odd real N, two real transforms (k, k + 1) per complex transform
-const void *bluestein_kernel(int kind, bool pair);
+// pair: odd real N, two real transforms (k, k + 1) per complex transform; mb: transforms
+// along M per tile (1, 2 or 4)
+const void *bluestein_kernel(int kind, bool pair, int mb);
+int bluestein_pad(int L, int mb); // spare shared elements after every 16
 int bluestein_threads(int L); // threads per transform of the length-L tile
 int bluestein_stages(int L);  // Stockham stages of the length-L transform
 int bluestein_radix(int L, int s);

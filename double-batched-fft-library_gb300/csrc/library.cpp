@@ -301,6 +301,11 @@ static bool ptc_supported_host(int P) {
 // and every warp of the block must be full.  NVRTC kernels (user callbacks) keep the
 // CUDA-core stage and its table.
 static bool tc_prime(int prec, int P) { return prec == 4 && ptc_supported_host(P); }
+// A prime complex length 17..47 runs its one radix-P butterfly per transform in registers
+// on the compile-time tiles of the other lengths (cover tiles), one thread per transform,
+// without copy stages around it (same rule as reg_prime_length() in
+// gen_specializations.py).
+static bool reg_prime_length(int nc) { return ptc_supported_host(nc) && nc <= 47; }
 // shared-memory elements the generic stage of radix P needs after the data buffers
 // (`tc_ok`: the kernel has the tensor-core stages, i.e. it is not an NVRTC kernel)
 static int gen_shared_elems(int prec, int P, bool tc_ok) {
@@ -597,8 +602,12 @@ static int vector_width(int prec, std::vector<int> const &rad) {
 // (consecutive threads load consecutive elements: 32-byte sectors when M = 1); ties go to
 // more threads.  The tensor-core prime stages use every warp of the block and do not count,
 // but with one of them T is at most 4 x its butterflies per transform where possible, so
-// that a block of 256 threads holds at least 64 of its butterflies (8 per warp).
-static int tile_threads(int nc, const int *rad, int L, int V) {
+// that a block of 256 threads holds at least 64 of its butterflies (8 per warp).  `reg`:
+// the prime length runs in registers on one thread per transform (reg_prime_length).
+static int tile_threads(int nc, const int *rad, int L, int V, bool reg = false) {
+    if (reg) {
+        return 1;
+    }
     auto counts = [](int r) { return !(r > 16 && ptc_supported_host(r)); };
     int nbmax = 1;
     int tcap = 256;
@@ -913,7 +922,9 @@ static pass make_bluestein_pass(pass_request const &q, pass ps, int flags, int N
     bool const pair = (ps.kind == kind_r2c_full || ps.kind == kind_c2r_full) && K >= 2 &&
                       (flags & (flag_adj_r2c | flag_adj_c2r)) == 0;
     long long const Kt = pair ? (K + 1) / 2 : K; // transforms along K of the tiles
-    int const Mb = static_cast<int>(std::min<long long>(M, 4));
+    // compile-time tile widths 1, 2, 4 (M = 3 in one tile of 4, as before in-place real
+    // transforms need the whole M range in one tile)
+    int const Mb = M >= 3 ? 4 : static_cast<int>(M);
     int const Kb =
         static_cast<int>(std::max<long long>(1, std::min<long long>(256 / T / Mb, Kt)));
     fft_params &p = ps.p;
@@ -947,7 +958,7 @@ static pass make_bluestein_pass(pass_request const &q, pass ps, int flags, int N
     // half-warp phases) leave one wavefront per 16 lanes except for L = 512, Mb = 1 (+20 %)
     int const E = Mb * Kb * L;
     p.pad_shift = 4;
-    p.pad_add = L == 512 && Mb % 2 == 0 ? 2 : 1;
+    p.pad_add = bluestein_pad(L, Mb);
     p.buf_elems = E + (E >> 4) * p.pad_add + p.pad_add;
     p.sw_a = 30;
     p.scale = 1.0;
@@ -1022,7 +1033,7 @@ static pass make_bluestein_pass(pass_request const &q, pass ps, int flags, int N
     ps.smem = static_cast<std::size_t>(p.buf_elems + TW) * 8; // tile buffer + stage twiddles
     ps.V = 1;
     ps.inplace_ok = q.type == BBFFT_C2C || Mb >= M;
-    ps.func = bluestein_kernel(ps.kind, pair);
+    ps.func = bluestein_kernel(ps.kind, pair, Mb);
     if (!ps.func) {
         throw status_error(BBFFT_INTERNAL_ERROR, "Bluestein kernel not found");
     }
@@ -1255,10 +1266,29 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         } else if (!q.runtime_only) {
             // plans of the other lengths (not ragged items: the persistent kernel cannot
             // call these tiles, and the runtime engine needs its own blocking)
-            cover_id = cover_ct_lookup(q.prec, ps.kind, Nc, Tt, rad.data(), L);
+            std::vector<int> core = choose_radices(Nc);
+            if (q.radices.empty() && !te_rad && reqT <= 0 && reg_prime_length(Nc)) {
+                // the prime stage in registers: no copy stages around it
+                if (is_real && !post && core.size() == 1) {
+                    core.push_back(1);
+                }
+                int const Lr = static_cast<int>(core.size());
+                int const Tr = tile_threads(Nc, core.data(), Lr, 1, true);
+                cover_id = cover_ct_lookup(q.prec, ps.kind, Nc, Tr, core.data(), Lr);
+                if (cover_id >= 0) {
+                    rad = core;
+                    L = Lr;
+                    T = Tr;
+                }
+            }
+            if (cover_id < 0) {
+                cover_id = cover_ct_lookup(q.prec, ps.kind, Nc, Tt, rad.data(), L);
+                if (cover_id >= 0) {
+                    T = Tt;
+                }
+            }
             if (cover_id >= 0) {
                 ct = &cover_ct_table[cover_id];
-                T = Tt;
             }
         }
     }

@@ -66,8 +66,10 @@ def test_ragged_small_batch(bb, po, torch_cuda, use_graph, form):
 
 
 def test_ragged_benchmark_batch_graph_replay(bb, po, torch_cuda):
-    """The 10^4-transform batch: two graph replays give identical results; a seeded
-    sample of 400 transforms matches the FP64 DFT."""
+    """The 10^4-transform batch: two graph replays give identical results, the grid form
+    the same bits, the class form the same to rounding; every one of the 10^4 transforms
+    of the persistent form (bit-equal to the grid form's) and a seeded sample of 400 of
+    the class form's match the FP64 DFT."""
     torch = torch_cuda
     specs, x, y, items = make_batch(bb, torch, 10000, seed=4)
     r = bb.Ragged(items)
@@ -92,6 +94,7 @@ def test_ragged_benchmark_batch_graph_replay(bb, po, torch_cuda):
     r.execute(s, use_graph=True)
     torch.cuda.synchronize()
     assert float(torch.linalg.vector_norm(y - first) / torch.linalg.vector_norm(first)) <= 1e-6
+    check_items(bb, po, specs, x, first, range(len(specs)))
     rng = np.random.default_rng(5)
     check_items(bb, po, specs, x, y, rng.choice(len(specs), 400, replace=False))
 
