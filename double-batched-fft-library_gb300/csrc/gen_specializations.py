@@ -77,18 +77,24 @@ def choose_radices(nc):
 BIG_PRIMES = {17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61}
 
 
-# A prime complex length 17..47 (c2c N = P, real N = 2P or odd N = P) runs its one
-# radix-P butterfly per transform in registers on one thread (dft<P> with literal
-# coefficients), without the copy stages around it: the tensor-core form needs shared
-# memory on both sides and several butterflies per warp, which such lengths do not have.
-# (Measured: with two or more butterflies per transform, 2P or 4P, the tensor-core form
-# stayed faster.)
+# A complex length k * P with a prime P = 17..47 and k <= 4 runs its radix-P butterflies in
+# registers, one per thread (dft<P> with literal coefficients), as the FIRST stage on
+# k threads per transform, followed by the radix-k stage and no copy stages: the
+# tensor-core form needs shared memory on both sides and several butterflies per warp,
+# which such lengths do not have.  (A first try with the prime stage last on 6 threads per
+# transform, most of them idle in that stage, was slower than the tensor-core form.)
 REG_PRIME_MAX = 47
 
 
 def reg_prime_length(nc):
     """Same rule as reg_prime_length() in library.cpp."""
-    return nc in BIG_PRIMES and nc <= REG_PRIME_MAX
+    return any(nc % p == 0 and nc // p <= 4 for p in BIG_PRIMES if p <= REG_PRIME_MAX)
+
+
+def reg_prime_radices(nc):
+    """[P] + the radices of k = nc / P (prime stage first)."""
+    p = [q for q in sorted(BIG_PRIMES) if nc % q == 0][0]
+    return [p] + (choose_radices(nc // p) if nc > p else [])
 
 
 def tile_threads(nc, rad, V=1, reg=False):
@@ -100,10 +106,10 @@ def tile_threads(nc, rad, V=1, reg=False):
     transform: 32-byte sectors when M = 1); ties go to more threads.  The tensor-core
     prime stages use every warp of the block and do not count, but with one of them T is
     at most 4 x its butterflies per transform where possible, so that a block of 256
-    threads holds at least 64 of its butterflies (8 per warp).  `reg`: the prime length runs
-    in registers on one thread per transform (reg_prime_length)."""
+    threads holds at least 64 of its butterflies (8 per warp).  `reg`: the prime stage runs
+    in registers, one butterfly per thread: nc / P threads (reg_prime_length)."""
     if reg:
-        return 1
+        return nc // rad[0]
     tc = BIG_PRIMES
     nbmax = max([nc // r for r in rad if r not in tc] + [1])
     tcap = min([4 * (nc // r) for r in rad if r in tc] + [256])
@@ -131,8 +137,8 @@ def stage_list(nc, kind, ragged=False, reg_ok=False):
     of make_1d_pass in library.cpp; `ragged`: a compile-time tile, i.e. a pass of a ragged
     batch or a plan on a tile kernel; `reg_ok`: a cover tile, whose prime stage may run in
     registers)."""
-    rad = choose_radices(nc)
     reg = ragged and reg_ok and reg_prime_length(nc)
+    rad = reg_prime_radices(nc) if reg else choose_radices(nc)
     if rad[0] not in UNROLLED and not reg:
         rad = [1] + rad
     real = kind != 0
@@ -233,8 +239,8 @@ def ragged_entries():
 
 def reg_prime_tile(nc, rad):
     """A cover tile whose prime stage runs in registers (stage_list with reg_ok): the
-    prime is its last radix and no copy stage precedes it."""
-    return reg_prime_length(nc) and rad[0] != 1 and any(r in BIG_PRIMES for r in rad)
+    prime is its first radix."""
+    return reg_prime_length(nc) and rad[0] in BIG_PRIMES
 
 
 def tile_min_blocks(rad, reg=False):

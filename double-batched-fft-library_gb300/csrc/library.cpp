@@ -301,11 +301,18 @@ static bool ptc_supported_host(int P) {
 // and every warp of the block must be full.  NVRTC kernels (user callbacks) keep the
 // CUDA-core stage and its table.
 static bool tc_prime(int prec, int P) { return prec == 4 && ptc_supported_host(P); }
-// A prime complex length 17..47 runs its one radix-P butterfly per transform in registers
-// on the compile-time tiles of the other lengths (cover tiles), one thread per transform,
-// without copy stages around it (same rule as reg_prime_length() in
-// gen_specializations.py).
-static bool reg_prime_length(int nc) { return ptc_supported_host(nc) && nc <= 47; }
+// A complex length k * P with a prime P = 17..47 and k <= 4 runs its radix-P butterflies in
+// registers on the compile-time tiles of the other lengths (cover tiles): the prime stage
+// first, one butterfly per thread on k threads per transform, then the radix-k stage, no
+// copy stages (same rule as reg_prime_length() in gen_specializations.py).  Returns P or 0.
+static int reg_prime_length(int nc) {
+    for (int P = 17; P <= 47; ++P) {
+        if (ptc_supported_host(P) && nc % P == 0 && nc / P <= 4) {
+            return P;
+        }
+    }
+    return 0;
+}
 // shared-memory elements the generic stage of radix P needs after the data buffers
 // (`tc_ok`: the kernel has the tensor-core stages, i.e. it is not an NVRTC kernel)
 static int gen_shared_elems(int prec, int P, bool tc_ok) {
@@ -603,10 +610,11 @@ static int vector_width(int prec, std::vector<int> const &rad) {
 // more threads.  The tensor-core prime stages use every warp of the block and do not count,
 // but with one of them T is at most 4 x its butterflies per transform where possible, so
 // that a block of 256 threads holds at least 64 of its butterflies (8 per warp).  `reg`:
-// the prime length runs in registers on one thread per transform (reg_prime_length).
+// the prime stage runs in registers, one butterfly per thread: nc / P threads
+// (reg_prime_length).
 static int tile_threads(int nc, const int *rad, int L, int V, bool reg = false) {
     if (reg) {
-        return 1;
+        return nc / rad[0];
     }
     auto counts = [](int r) { return !(r > 16 && ptc_supported_host(r)); };
     int nbmax = 1;
@@ -1266,9 +1274,14 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         } else if (!q.runtime_only) {
             // plans of the other lengths (not ragged items: the persistent kernel cannot
             // call these tiles, and the runtime engine needs its own blocking)
-            std::vector<int> core = choose_radices(Nc);
-            if (q.radices.empty() && !te_rad && reqT <= 0 && reg_prime_length(Nc)) {
-                // the prime stage in registers: no copy stages around it
+            int const Preg = reg_prime_length(Nc);
+            if (q.radices.empty() && !te_rad && reqT <= 0 && Preg > 0) {
+                // the prime stage in registers, first, then the radices of Nc / P
+                std::vector<int> core{Preg};
+                if (Nc > Preg) {
+                    std::vector<int> rest = choose_radices(Nc / Preg);
+                    core.insert(core.end(), rest.begin(), rest.end());
+                }
                 if (is_real && !post && core.size() == 1) {
                     core.push_back(1);
                 }
