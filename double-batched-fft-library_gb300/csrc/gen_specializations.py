@@ -77,18 +77,20 @@ def choose_radices(nc):
 BIG_PRIMES = {17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61}
 
 
-# A complex length k * P with a prime P = 17..47 and k <= 4 runs its radix-P butterflies in
-# registers, one per thread (dft<P> with literal coefficients), as the FIRST stage on
-# k threads per transform, followed by the radix-k stage and no copy stages: the
-# tensor-core form needs shared memory on both sides and several butterflies per warp,
-# which such lengths do not have.  (A first try with the prime stage last on 6 threads per
-# transform, most of them idle in that stage, was slower than the tensor-core form.)
+# A complex length k * P with a prime P = 17..47 and k <= REG_PRIME_KMAX runs its radix-P
+# butterflies in registers, one per thread (dft<P> with literal coefficients), as the
+# FIRST stage on k threads per transform, followed by the stages of k and no copy stages:
+# the tensor-core form needs shared memory on both sides and several butterflies per warp,
+# and leaves threads idle at so few butterflies per transform.  (A first try with the prime
+# stage last on 6 threads per transform, most of them idle in that stage, was slower than
+# the tensor-core form.)
 REG_PRIME_MAX = 47
+REG_PRIME_KMAX = 16
 
 
 def reg_prime_length(nc):
     """Same rule as reg_prime_length() in library.cpp."""
-    return any(nc % p == 0 and nc // p <= 4 for p in BIG_PRIMES if p <= REG_PRIME_MAX)
+    return any(nc % p == 0 and nc // p <= REG_PRIME_KMAX for p in BIG_PRIMES if p <= REG_PRIME_MAX)
 
 
 def reg_prime_radices(nc):

@@ -301,13 +301,14 @@ static bool ptc_supported_host(int P) {
 // and every warp of the block must be full.  NVRTC kernels (user callbacks) keep the
 // CUDA-core stage and its table.
 static bool tc_prime(int prec, int P) { return prec == 4 && ptc_supported_host(P); }
-// A complex length k * P with a prime P = 17..47 and k <= 4 runs its radix-P butterflies in
-// registers on the compile-time tiles of the other lengths (cover tiles): the prime stage
-// first, one butterfly per thread on k threads per transform, then the radix-k stage, no
-// copy stages (same rule as reg_prime_length() in gen_specializations.py).  Returns P or 0.
+// A complex length k * P with a prime P = 17..47 and k <= 16 runs its radix-P butterflies
+// in registers on the compile-time tiles of the other lengths (cover tiles): the prime
+// stage first, one butterfly per thread on k threads per transform, then the stages of k,
+// no copy stages (same rule as reg_prime_length() in gen_specializations.py).  Returns P
+// or 0.
 static int reg_prime_length(int nc) {
     for (int P = 17; P <= 47; ++P) {
-        if (ptc_supported_host(P) && nc % P == 0 && nc / P <= 4) {
+        if (ptc_supported_host(P) && nc % P == 0 && nc / P <= 16) {
             return P;
         }
     }
