@@ -84,18 +84,30 @@ BIG_PRIMES = {17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61}
 # and leaves threads idle at so few butterflies per transform.  (A first try with the prime
 # stage last on 6 threads per transform, most of them idle in that stage, was slower than
 # the tensor-core form.)
-REG_PRIME_MAX = 47
-REG_PRIME_KMAX = 16
+REG_PRIME_MAX = 61
+REG_PRIME_KMAX = 32
+
+
+def reg_prime_of(nc):
+    """The prime P of a register-prime length (smallest prime factor >= 17 of nc, with
+    k = nc / P <= REG_PRIME_KMAX and no prime factor >= 17 in k), or 0; same rule as
+    reg_prime_length() in library.cpp."""
+    big = [q for q in sorted(BIG_PRIMES) if nc % q == 0]
+    if not big or big[0] > REG_PRIME_MAX:
+        return 0
+    p, k = big[0], nc // big[0]
+    if k > REG_PRIME_KMAX or any(k % q == 0 for q in BIG_PRIMES) or largest_prime_factor(k) > 16:
+        return 0
+    return p
 
 
 def reg_prime_length(nc):
-    """Same rule as reg_prime_length() in library.cpp."""
-    return any(nc % p == 0 and nc // p <= REG_PRIME_KMAX for p in BIG_PRIMES if p <= REG_PRIME_MAX)
+    return reg_prime_of(nc) > 0
 
 
 def reg_prime_radices(nc):
     """[P] + the radices of k = nc / P (prime stage first)."""
-    p = [q for q in sorted(BIG_PRIMES) if nc % q == 0][0]
+    p = reg_prime_of(nc)
     return [p] + (choose_radices(nc // p) if nc > p else [])
 
 
@@ -227,7 +239,8 @@ def ragged_entries():
     out = []
     for kind, ncs in ((0, range(16, 513, 8)), (1, range(8, 257, 4))):
         for nc in ncs:
-            rad, T = stage_list(nc, kind, ragged=True)
+            # the prime stage in registers up to P = 47 (the units compile for 128 registers)
+            rad, T = stage_list(nc, kind, ragged=True, reg_ok=0 < reg_prime_of(nc) <= 47)
             if any(r not in UNROLLED and r not in BIG_PRIMES for r in rad):
                 continue
             out.append((4, kind, nc, T, rad, 1))
@@ -248,9 +261,11 @@ def reg_prime_tile(nc, rad):
 def tile_min_blocks(rad, reg=False):
     """Resident 256-thread CTAs the register budget of a tile kernel is sized for: 3 (80
     registers) with a tensor-core prime stage, whose tiles are otherwise limited by the
-    latency of 2 CTAs per SM at 128 registers; 2 for the others (and for a prime stage in
-    registers, which holds up to 47 complex values per thread)."""
-    return 3 if any(r in BIG_PRIMES for r in rad) and not reg else 2
+    latency of 2 CTAs per SM at 128 registers; 2 for the others and for a prime stage in
+    registers up to P = 47 (47 complex values per thread); 1 (255 registers) for P = 53..61."""
+    if reg:
+        return 1 if max(rad) > 47 else 2
+    return 3 if any(r in BIG_PRIMES for r in rad) else 2
 
 
 def largest_prime_factor(n):
@@ -358,18 +373,21 @@ def ragged_units(outdir):
                '#include "engine_ct.cuh"', '#include "kernels.hpp"', '', 'namespace gbfft {', '']
         for i in sorted(idx):
             prec, kind, nc, T, rad, V = ents[i]
-            targs = 'float, %d, %d, %d, %d, %s' % (kind, nc, T, V, ', '.join(map(str, rad)))
+            reg = reg_prime_tile(nc, rad)
+            targs = 'float, %d, %d, %d, %d, false, %s, %s' % (kind, nc, T, V, 'true' if reg else 'false',
+                                                          ', '.join(map(str, rad)))
+            minb = tile_min_blocks(rad, reg)
             src += ['__device__ __noinline__ void ragged_ct_%d(const fft_params &p, long long tile) {' % i,
-                    '    fft_tile_ct_ragged<%s>(p, tile);' % targs,
+                    '    fft_tile_ct_ragged_t<%s>(p, tile);' % targs,
                     '}', '',
-                    '__global__ void __launch_bounds__(256, %d) ragged_class_ct_%d(const ragged_item_dev *__restrict__ items,' % (tile_min_blocks(rad), i),
+                    '__global__ void __launch_bounds__(256, %d) ragged_class_ct_%d(const ragged_item_dev *__restrict__ items,' % (minb, i),
                     '                                                        const int2 *__restrict__ units) {',
                     '    __shared__ __align__(16) fft_params s_p;',
                     '    const int2 un = stage_unit_params(items, units, s_p);',
-                    '    fft_tile_ct_ragged<%s>(s_p, un.y);' % targs,
+                    '    fft_tile_ct_ragged_t<%s>(s_p, un.y);' % targs,
                     '}', '',
-                    '__global__ void __launch_bounds__(256, %d) plan_ct_%d(const __grid_constant__ fft_params p) {' % (tile_min_blocks(rad), i),
-                    '    fft_tile_ct_ragged<%s>(p, blockIdx.x);' % targs,
+                    '__global__ void __launch_bounds__(256, %d) plan_ct_%d(const __grid_constant__ fft_params p) {' % (minb, i),
+                    '    fft_tile_ct_ragged_t<%s>(p, blockIdx.x);' % targs,
                     '}', '']
         for kname in ('ragged_class_ct', 'plan_ct'):
             src += ['const void *%s_kernel_%d(int vid) {' % (kname, g), '    switch (vid) {']

@@ -301,16 +301,26 @@ static bool ptc_supported_host(int P) {
 // and every warp of the block must be full.  NVRTC kernels (user callbacks) keep the
 // CUDA-core stage and its table.
 static bool tc_prime(int prec, int P) { return prec == 4 && ptc_supported_host(P); }
-// A complex length k * P with a prime P = 17..47 and k <= 16 runs its radix-P butterflies
-// in registers on the compile-time tiles of the other lengths (cover tiles): the prime
-// stage first, one butterfly per thread on k threads per transform, then the stages of k,
-// no copy stages (same rule as reg_prime_length() in gen_specializations.py).  Returns P
-// or 0.
+// A complex length k * P (P the smallest prime factor >= 17, P <= 61, k <= 32 without a
+// prime factor >= 17) runs its radix-P butterflies in registers on the compile-time tiles
+// of the other lengths (cover tiles): the prime stage first, one butterfly per thread on
+// k threads per transform, then the stages of k, no copy stages (same rule as
+// reg_prime_of() in gen_specializations.py).  Returns P or 0.
 static int reg_prime_length(int nc) {
-    for (int P = 17; P <= 47; ++P) {
-        if (ptc_supported_host(P) && nc % P == 0 && nc / P <= 16) {
-            return P;
+    for (int P = 17; P <= 61; ++P) {
+        if (nc % P != 0 || !ptc_supported_host(P)) {
+            continue; // P: the smallest prime factor >= 17 of nc
         }
+        int const k = nc / P;
+        if (k > 32) {
+            return 0;
+        }
+        for (int q = 17; q <= k; ++q) {
+            if (ptc_supported_host(q) && k % q == 0) {
+                return 0; // k has a prime factor >= 17 (k <= 32: 17..31)
+            }
+        }
+        return P;
     }
     return 0;
 }
@@ -1246,6 +1256,33 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
     // ragged batches, and plans of lengths without a compile-time plan kernel
     int ragged_vid = -1;
     int cover_id = -1;
+    // a length whose prime stage runs in registers (reg_prime_length): the prime stage
+    // first, then the radices of Nc / P (no copy stages; real single stages keep theirs)
+    int const Preg = (q.radices.empty() && !te_rad && reqT <= 0) ? reg_prime_length(Nc) : 0;
+    std::vector<int> rad_reg;
+    if (Preg > 0) {
+        rad_reg.push_back(Preg);
+        if (Nc > Preg) {
+            std::vector<int> rest = choose_radices(Nc / Preg);
+            rad_reg.insert(rad_reg.end(), rest.begin(), rest.end());
+        }
+        if (is_real && !post && rad_reg.size() == 1) {
+            rad_reg.push_back(1);
+        }
+    }
+    int const L_reg = static_cast<int>(rad_reg.size());
+    int const T_reg = Preg > 0 ? tile_threads(Nc, rad_reg.data(), L_reg, 1, true) : 0;
+    if (!has_cb && !ct && q.prec == 4 && Preg > 0 && Preg <= 47) {
+        // the ragged tiles run the prime stage in registers up to P = 47
+        ragged_vid = ragged_ct_lookup(q.prec, ps.kind, Nc, T_reg, 1, rad_reg.data(), L_reg);
+        if (ragged_vid >= 0) {
+            rad = rad_reg;
+            L = L_reg;
+            T = T_reg;
+            V = 1;
+            ct = &ragged_ct_table[ragged_vid];
+        }
+    }
     if (!has_cb && !ct && q.prec == 4) {
         // compile-time tiles choose their own threads per transform (tile_threads)
         int const Tt = reqT > 0 ? T : tile_threads(Nc, rad.data(), L, 1);
@@ -1275,24 +1312,12 @@ pass make_1d_pass(pass_request const &q, int device, bbfft_cache_s *cache) {
         } else if (!q.runtime_only) {
             // plans of the other lengths (not ragged items: the persistent kernel cannot
             // call these tiles, and the runtime engine needs its own blocking)
-            int const Preg = reg_prime_length(Nc);
-            if (q.radices.empty() && !te_rad && reqT <= 0 && Preg > 0) {
-                // the prime stage in registers, first, then the radices of Nc / P
-                std::vector<int> core{Preg};
-                if (Nc > Preg) {
-                    std::vector<int> rest = choose_radices(Nc / Preg);
-                    core.insert(core.end(), rest.begin(), rest.end());
-                }
-                if (is_real && !post && core.size() == 1) {
-                    core.push_back(1);
-                }
-                int const Lr = static_cast<int>(core.size());
-                int const Tr = tile_threads(Nc, core.data(), Lr, 1, true);
-                cover_id = cover_ct_lookup(q.prec, ps.kind, Nc, Tr, core.data(), Lr);
+            if (Preg > 0) {
+                cover_id = cover_ct_lookup(q.prec, ps.kind, Nc, T_reg, rad_reg.data(), L_reg);
                 if (cover_id >= 0) {
-                    rad = core;
-                    L = Lr;
-                    T = Tr;
+                    rad = rad_reg;
+                    L = L_reg;
+                    T = T_reg;
                 }
             }
             if (cover_id < 0) {
@@ -2312,6 +2337,10 @@ const char *bbfft_last_error(void) {
     return gbfft::tl_fixed_active ? gbfft::tl_fixed_error : gbfft::tl_error.c_str();
 }
 const char *bbfft_version(void) { return "bbfft-gb300 0.1.0 (sm_103a)"; }
+
+// Internal (no header): the prime P of a length whose radix-P stage the compile-time tiles
+// run in registers, or 0 — for the check that the host and the kernel generator agree.
+BBFFT_GB300_API int gbfft_internal_reg_prime(int nc) { return gbfft::reg_prime_length(nc); }
 
 int bbfft_default_istride(uint32_t dim, const size_t shape[BBFFT_MAX_TENSOR_DIM], int32_t type,
                           int inplace, size_t stride_out[BBFFT_MAX_TENSOR_DIM]) {
