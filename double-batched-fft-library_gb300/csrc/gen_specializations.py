@@ -124,6 +124,9 @@ def tile_threads(nc, rad, V=1, reg=False):
     in registers, one butterfly per thread: nc / P threads (reg_prime_length)."""
     if reg:
         return nc // rad[0]
+    if len(rad) == 2 and rad[1] == 1:
+        # one butterfly stage and the copy stage: every thread one butterfly in the first
+        return nc // rad[0]
     tc = BIG_PRIMES
     nbmax = max([nc // r for r in rad if r not in tc] + [1])
     tcap = min([4 * (nc // r) for r in rad if r in tc] + [256])
@@ -258,13 +261,17 @@ def reg_prime_tile(nc, rad):
     return reg_prime_length(nc) and rad[0] in BIG_PRIMES
 
 
-def tile_min_blocks(rad, reg=False):
+def tile_min_blocks(rad, reg=False, cover=False):
     """Resident 256-thread CTAs the register budget of a tile kernel is sized for: 3 (80
     registers) with a tensor-core prime stage, whose tiles are otherwise limited by the
-    latency of 2 CTAs per SM at 128 registers; 2 for the others and for a prime stage in
-    registers up to P = 47 (47 complex values per thread); 1 (255 registers) for P = 53..61."""
+    latency of 2 CTAs per SM at 128 registers, and for the cover tiles without a prime
+    stage (measured at 21 % achieved occupancy with 2; at 80 registers 7 of 354 spill, at
+    most 16 bytes); 2 for the others and for a prime stage in registers up to P = 47
+    (47 complex values per thread); 1 (255 registers) for P = 53..61."""
     if reg:
         return 1 if max(rad) > 47 else 2
+    if cover:
+        return 3
     return 3 if any(r in BIG_PRIMES for r in rad) else 2
 
 
@@ -310,7 +317,7 @@ def cover_units(outdir):
             reg = reg_prime_tile(nc, rad)
             targs = 'float, %d, %d, %d, %d, %s, %s, %s' % (kind, nc, T, V, two, 'true' if reg else 'false',
                                                        ', '.join(map(str, rad)))
-            src += ['__global__ void __launch_bounds__(256, %d) cover_ct_%d(const __grid_constant__ fft_params p) {' % (tile_min_blocks(rad, reg), i),
+            src += ['__global__ void __launch_bounds__(256, %d) cover_ct_%d(const __grid_constant__ fft_params p) {' % (tile_min_blocks(rad, reg, cover=True), i),
                     '    fft_tile_ct_ragged_t<%s>(p, blockIdx.x);' % targs, '}', '']
         src += ['const void *cover_ct_kernel_%d(int i) {' % g, '    switch (i) {']
         for i in idx:
@@ -327,7 +334,9 @@ def cover_units(outdir):
         host += ['    case %d:' % g, '        return cover_ct_kernel_%d(i);' % g]
     host += ['    }', '    return nullptr;', '}', '', 'extern const ct_entry cover_ct_table[] = {']
     for prec, kind, nc, T, rad, V in ents:
-        host.append('    {%d, %d, %d, %d, %d, %d, {%s}, nullptr, 2},' % (prec, kind, nc, T, V, len(rad), ', '.join(map(str, rad))))
+        minb = tile_min_blocks(rad, reg_prime_tile(nc, rad), cover=True)
+        host.append('    {%d, %d, %d, %d, %d, %d, {%s}, nullptr, %d},' % (prec, kind, nc, T, V, len(rad),
+                                                                    ', '.join(map(str, rad)), minb))
     host += ['};', 'static const int kCoverSize = %d;' % len(ents), '',
              'int cover_ct_lookup(int prec, int kind, int nc, int T, const int *rad, int L) {',
              '    for (int i = 0; i < kCoverSize; ++i) {',
@@ -418,7 +427,9 @@ def ragged_units(outdir):
         host += ['    return f;', '}', '']
     host += ['extern const ct_entry ragged_ct_table[] = {']
     for prec, kind, nc, T, rad, V in ents:
-        host.append('    {%d, %d, %d, %d, %d, %d, {%s}, nullptr, 2},' % (prec, kind, nc, T, V, len(rad), ', '.join(map(str, rad))))
+        minb = tile_min_blocks(rad, reg_prime_tile(nc, rad), cover=True)
+        host.append('    {%d, %d, %d, %d, %d, %d, {%s}, nullptr, %d},' % (prec, kind, nc, T, V, len(rad),
+                                                                    ', '.join(map(str, rad)), minb))
     host += ['};', 'static const int kRaggedSize = %d;' % len(ents), '',
              'int ragged_ct_lookup(int prec, int kind, int nc, int T, int V, const int *rad, int L) {',
              '    for (int i = 0; i < kRaggedSize; ++i) {',

@@ -624,7 +624,9 @@ static int vector_width(int prec, std::vector<int> const &rad) {
 // the prime stage runs in registers, one butterfly per thread: nc / P threads
 // (reg_prime_length).
 static int tile_threads(int nc, const int *rad, int L, int V, bool reg = false) {
-    if (reg) {
+    if (reg || (L == 2 && rad[1] == 1)) {
+        // a register prime stage, or one butterfly stage and the copy stage: one butterfly
+        // per thread in the first stage
         return nc / rad[0];
     }
     auto counts = [](int r) { return !(r > 16 && ptc_supported_host(r)); };
