@@ -250,7 +250,7 @@ template <int Kind, int L, bool PAIR, int MB> __device__ __forceinline__ void ti
 }
 
 template <int Kind, bool PAIR, int MB>
-__global__ void __launch_bounds__(256, 4) bluestein_kernel(const __grid_constant__ fft_params p) {
+__global__ void __launch_bounds__(256, 5) bluestein_kernel(const __grid_constant__ fft_params p) {
     switch (p.bL) {
     case 256:
         tiles<Kind, 256, PAIR, MB>(p);
