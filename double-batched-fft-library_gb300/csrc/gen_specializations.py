@@ -385,7 +385,10 @@ def ragged_units(outdir):
             reg = reg_prime_tile(nc, rad)
             targs = 'float, %d, %d, %d, %d, false, %s, %s' % (kind, nc, T, V, 'true' if reg else 'false',
                                                           ', '.join(map(str, rad)))
-            minb = tile_min_blocks(rad, reg)
+            # V = 1 tiles without a prime stage: 3 resident CTAs (80 registers; 1 of 88 spills,
+            # 12 bytes); the V = 2 / 4 variants hold more values per thread and keep 2
+            minb = 3 if V == 1 and not reg and not any(r in BIG_PRIMES for r in rad) else \
+                tile_min_blocks(rad, reg)
             src += ['__device__ __noinline__ void ragged_ct_%d(const fft_params &p, long long tile) {' % i,
                     '    fft_tile_ct_ragged_t<%s>(p, tile);' % targs,
                     '}', '',
