@@ -488,6 +488,9 @@ __device__ __forceinline__ void ct_stage_prime(const Ctx &c, int j) {
 }
 
 // One in-place Stockham stage with compile-time sizes (see engine.cuh for the formulas).
+// A prime radix 17..61 takes the shared-memory / tensor-core form (ct_stage_prime) unless
+// the tile runs it in registers (Ctx::reg_prime): then it is an ordinary stage whose
+// butterfly is dft<P> (radix.cuh, pair sums with literal coefficients), one per thread.
 template <int P, int NS, bool SRC_G, bool DST_G, class Ctx, class R, int NC, int TT, int V>
 __device__ __forceinline__ void ct_stage(const Ctx &c, int j) {
     if constexpr (ct_big_prime(P) && !Ctx::reg_prime) {
