@@ -36,3 +36,23 @@ def test_register_prime_stage_lists():
         assert prod == nc
     rad, T = gen.stage_list(17, 2, ragged=True, reg_ok=True)
     assert rad == [17, 1] and T == 1
+
+
+def test_every_generated_tile_is_consistent():
+    """Every compile-time tile the generator emits (cover and ragged sets): its radices
+    multiply to the complex length (copy stages are radix 1), its threads per transform
+    fit a 256-thread block, a register prime tile puts its prime first on nc / P threads,
+    and the resident-CTA budget matches the stage kinds."""
+    for kind_set, ents in (('cover', gen.cover_entries()), ('ragged', gen.ragged_entries())):
+        for prec, kind, nc, T, rad, V in ents:
+            prod = 1
+            for r in rad:
+                prod *= r
+            assert prod == nc, (kind_set, kind, nc, rad)
+            assert 1 <= T <= 256 and T * V <= 256, (kind_set, kind, nc, T, V)
+            reg = gen.reg_prime_tile(nc, rad)
+            if reg:
+                assert rad[0] == gen.reg_prime_of(nc) and T == nc // rad[0], (kind_set, nc, rad, T)
+                assert gen.tile_min_blocks(rad, reg) in (1, 2)
+            if kind_set == 'ragged' and reg:
+                assert rad[0] <= 47, (nc, rad)  # the ragged units compile for 128 registers
